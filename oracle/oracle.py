@@ -1,0 +1,133 @@
+"""ctypes loader for the C oracle (oracle/pdhg_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the CPU
+baseline leg of bench.py, never by the shipped package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (-ffp-contract=off keeps float ops unfused)."""
+    src = os.path.join(HERE, "pdhg_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+        subprocess.check_call(["gcc", "-O3", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+                               src, "-o", LIB_PATH, "-lm"])
+    return LIB_PATH
+
+
+class OracleConfig(C.Structure):
+    _fields_ = [("max_iterations", C.c_int32), ("tol_primal", C.c_float), ("tol_dual", C.c_float),
+                ("tol_gap", C.c_float), ("check_frequency", C.c_int32), ("step_tau", C.c_float),
+                ("step_sigma", C.c_float), ("enable_restart", C.c_uint8), ("enable_hybrid_polish", C.c_uint8)]
+
+
+class OraclePlainInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_int64), ("primal_objective", C.c_double),
+                ("last_norm_p", C.c_float), ("last_norm_d", C.c_float), ("best_combined", C.c_float),
+                ("checks", C.c_int64)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+    return _lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def config_from(cfg) -> OracleConfig:
+    """Copy the fields of any GpuPdhgConfig-like object."""
+    o = OracleConfig()
+    for name, _ in OracleConfig._fields_:
+        v = getattr(cfg, name)
+        setattr(o, name, int(v) if name in ("max_iterations", "check_frequency", "enable_restart",
+                                            "enable_hybrid_polish") else float(v))
+    return o
+
+
+def plain_pdhg(problem, cfg, threads: int = 0):
+    """Reference-semantics plain FP32 PDHG on the CPU.  Returns (x, y, info dict)."""
+    A = problem.A
+    m, n = problem.num_rows(), problem.num_cols()
+    x = np.zeros(n)
+    y = np.zeros(m)
+    info = OraclePlainInfo()
+    oc = config_from(cfg)
+    arrs = [np.ascontiguousarray(a) for a in (A.csc_col_ptr(), A.csc_row_ind(), A.csc_values(), problem.c,
+                                              problem.col_lower, problem.col_upper, problem.row_lower,
+                                              problem.row_upper)]
+    rc = lib().oracle_plain_pdhg(C.c_int64(m), C.c_int64(n), _p(arrs[0], C.c_int64), _p(arrs[1], C.c_int64),
+                                 _p(arrs[2], C.c_double), _p(arrs[3], C.c_double), _p(arrs[4], C.c_double),
+                                 _p(arrs[5], C.c_double), _p(arrs[6], C.c_double), _p(arrs[7], C.c_double),
+                                 C.byref(oc), _p(x, C.c_double), _p(y, C.c_double), C.byref(info), C.c_int(threads))
+    if rc != 0:
+        raise ValueError("oracle_plain_pdhg rejected its arguments")
+    return x, y, {k: getattr(info, k) for k, _ in OraclePlainInfo._fields_}
+
+
+def kkt(problem, x, y):
+    """FP64 relative KKT of (x, y) with y in the PDHG sign.  Returns dict."""
+    A = problem.A
+    out = np.zeros(6)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    lib().oracle_kkt(C.c_int64(problem.num_rows()), C.c_int64(problem.num_cols()), _p(A.csc_col_ptr(), C.c_int64),
+                     _p(A.csc_row_ind(), C.c_int64), _p(A.csc_values(), C.c_double), _p(problem.c, C.c_double),
+                     _p(problem.col_lower, C.c_double), _p(problem.col_upper, C.c_double),
+                     _p(problem.row_lower, C.c_double), _p(problem.row_upper, C.c_double), _p(x, C.c_double),
+                     _p(y, C.c_double), _p(out, C.c_double))
+    return dict(rel_primal=out[0], rel_dual=out[1], rel_gap=out[2], primal_obj=out[3], dual_obj=out[4],
+                abs_primal=out[5])
+
+
+def csr_spmv_f32(rp, ci, v, x):
+    rp, ci = np.ascontiguousarray(rp, np.int32), np.ascontiguousarray(ci, np.int32)
+    v, x = np.ascontiguousarray(v, np.float32), np.ascontiguousarray(x, np.float32)
+    y = np.zeros(rp.shape[0] - 1, np.float32)
+    lib().oracle_csr_spmv_f32(C.c_int(y.shape[0]), _p(rp, C.c_int), _p(ci, C.c_int), _p(v, C.c_float),
+                              _p(x, C.c_float), _p(y, C.c_float))
+    return y
+
+
+def csc_spmv_f32(cp, ri, v, y):
+    cp, ri = np.ascontiguousarray(cp, np.int32), np.ascontiguousarray(ri, np.int32)
+    v, y = np.ascontiguousarray(v, np.float32), np.ascontiguousarray(y, np.float32)
+    z = np.zeros(cp.shape[0] - 1, np.float32)
+    lib().oracle_csc_spmv_f32(C.c_int(z.shape[0]), _p(cp, C.c_int), _p(ri, C.c_int), _p(v, C.c_float),
+                              _p(y, C.c_float), _p(z, C.c_float))
+    return z
+
+
+def primal_update_f32(tau, c, aty, l, u, x):
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    tau, c, aty, l, u = map(f, (tau, c, aty, l, u))
+    x = f(x).copy()
+    xbar = np.zeros_like(x)
+    lib().oracle_primal_update_f32(C.c_int(x.shape[0]), _p(tau, C.c_float), _p(c, C.c_float), _p(aty, C.c_float),
+                                   _p(l, C.c_float), _p(u, C.c_float), _p(x, C.c_float), _p(xbar, C.c_float))
+    return x, xbar
+
+
+def dual_update_f32(sigma, axbar, rl, ru, y):
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    sigma, axbar, rl, ru = map(f, (sigma, axbar, rl, ru))
+    y = f(y).copy()
+    lib().oracle_dual_update_f32(C.c_int(y.shape[0]), _p(sigma, C.c_float), _p(axbar, C.c_float),
+                                 _p(rl, C.c_float), _p(ru, C.c_float), _p(y, C.c_float))
+    return y
