@@ -1,0 +1,217 @@
+/*
+ * sih_pdhg.h -- C ABI of the GB300 (sm_103a) PDHG LP engine.
+ *
+ * Drop-in boundary for the reference's GPU PDHG path (kavinR-11/refinery-optimizer):
+ * every entry point below names the reference interface it replaces.  The ABI
+ * uses plain pointers, sizes and POD structs only; no C++ or framework types
+ * cross it, and no entry point throws.  Every function returns an int status
+ * (SIH_PDHG_OK or an SIH_PDHG_ERR_* code); sih_pdhg_last_error() gives the
+ * message of the calling thread's last failure.
+ *
+ * Host pointers are used by the sih_pdhg_solve* / handle entry points; the
+ * sih_pdhg_launch_* entry points take DEVICE pointers and a cudaStream_t
+ * passed as void* (NULL = the legacy default stream), exactly like the
+ * reference's launch_* functions they replace.
+ */
+#ifndef SIH_PDHG_H
+#define SIH_PDHG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SIH_PDHG_ABI_VERSION 1
+
+/* ---- status codes of the ABI ------------------------------------------- */
+enum {
+    SIH_PDHG_OK = 0,
+    SIH_PDHG_ERR_INVALID_ARGUMENT = 1, /* bad size, NULL pointer, malformed CSC/CSR, bad config */
+    SIH_PDHG_ERR_NO_DEVICE = 2,        /* no CUDA device: the engine has no CPU fallback */
+    SIH_PDHG_ERR_CUDA = 3,             /* a CUDA runtime call or kernel launch failed */
+    SIH_PDHG_ERR_OUT_OF_MEMORY = 4,    /* device or pinned-host allocation failed */
+    SIH_PDHG_ERR_UNSUPPORTED = 5       /* valid request this build cannot serve (e.g. > 2^31-1 nnz) */
+};
+
+/* ---- values of sih::model::SolutionStatus (core/include/sih/model/solution.hpp:11-21) */
+enum {
+    SIH_STATUS_OPTIMAL = 0,
+    SIH_STATUS_INFEASIBLE = 1,
+    SIH_STATUS_UNBOUNDED = 2,
+    SIH_STATUS_TIME_LIMIT = 3,
+    SIH_STATUS_ITERATION_LIMIT = 4,
+    SIH_STATUS_NODE_LIMIT = 5,
+    SIH_STATUS_NUMERICAL_FAILURE = 6,
+    SIH_STATUS_INTERRUPTED = 7,
+    SIH_STATUS_UNKNOWN = 8
+};
+
+/*
+ * Same fields, order, types and defaults as sih::gpu::GpuPdhgConfig
+ * (core/include/sih/gpu/gpu_solver.hpp:12-22): int, 3 x float, int,
+ * 2 x float, 2 x bool (one byte each).  32 bytes on LP64.
+ */
+typedef struct sih_pdhg_config {
+    int32_t max_iterations;      /* 4000 */
+    float tol_primal;            /* 1e-4 */
+    float tol_dual;              /* 1e-4 */
+    float tol_gap;               /* 1e-4 (used by the mixed algorithm; the reference never reads it) */
+    int32_t check_frequency;     /* 25, must be > 0 */
+    float step_tau;              /* 0 = automatic */
+    float step_sigma;            /* 0 = automatic */
+    uint8_t enable_restart;      /* 1 */
+    uint8_t enable_hybrid_polish; /* 1 (read only by a hybrid caller, not by the PDHG solve) */
+} sih_pdhg_config;
+
+/*
+ * One LP as the reference's sih::model::Problem holds it
+ * (core/include/sih/model/problem.hpp:37-137, sparse_matrix.hpp:20-77):
+ *   minimize sense * (c^T x) + obj_offset   (sense 1 = Minimize, -1 = Maximize)
+ *   row_lower <= A x <= row_upper,  col_lower <= x <= col_upper
+ * A as CSC with int64 indices and float64 values (required) and optionally as
+ * CSR (NULL pointers = built here).  When given, the CSR must hold the same
+ * entries with columns ascending within each row (the order of
+ * SparseMatrix::from_triplets).  Infinite bounds are +-INFINITY or |v| >= 1e20.
+ */
+typedef struct sih_pdhg_problem {
+    int64_t num_rows;
+    int64_t num_cols;
+    int64_t num_nonzeros;
+    const int64_t* csc_col_ptr; /* [num_cols + 1] */
+    const int64_t* csc_row_ind; /* [num_nonzeros] */
+    const double* csc_values;   /* [num_nonzeros] */
+    const int64_t* csr_row_ptr; /* [num_rows + 1] or NULL */
+    const int64_t* csr_col_ind; /* [num_nonzeros] or NULL */
+    const double* csr_values;   /* [num_nonzeros] or NULL */
+    const double* c;            /* [num_cols] */
+    const double* col_lower;    /* [num_cols] */
+    const double* col_upper;    /* [num_cols] */
+    const double* row_lower;    /* [num_rows] */
+    const double* row_upper;    /* [num_rows] */
+    int32_t sense;
+    double obj_offset;
+} sih_pdhg_problem;
+
+/* Algorithms served by sih_pdhg_solve_ex. */
+enum {
+    SIH_PDHG_ALGO_PLAIN = 0, /* the reference's FP32 PDHG: fixed diagonal steps, its termination test */
+    SIH_PDHG_ALGO_MIXED = 1  /* restarted adaptive PDHG: Ruiz + Pock-Chambolle scaling, adaptive step,
+                                primal weight, KKT restarts; FP32 SpMV/updates, FP64 reductions */
+};
+
+/* Settings of the added entry points.  Fill with sih_pdhg_options_default(). */
+typedef struct sih_pdhg_options {
+    int32_t struct_size;       /* sizeof(sih_pdhg_options) */
+    int32_t algorithm;         /* SIH_PDHG_ALGO_* */
+    int32_t ruiz_iterations;   /* mixed: Ruiz passes (10) */
+    int32_t pock_chambolle;    /* mixed: 1 = apply the alpha=1 Pock-Chambolle pass */
+    int32_t eval_frequency;    /* mixed: iterations between restart/termination checks (64) */
+    int32_t compensated;       /* mixed: 0 off, 1 on near tolerance (default), 2 always */
+    int32_t dual_sign;         /* 0 = PDHG sign of the reference (row_duals = -simplex duals), 1 = simplex sign */
+    int32_t use_graph;         /* 1 = replay iteration blocks as CUDA graphs */
+    int32_t autotune;          /* 1 = time SpMV tile shapes once per matrix shape and keep the fastest */
+    int32_t verbose;           /* 0 */
+    double time_limit_sec;     /* <= 0: none */
+    double restart_sufficient; /* mixed: 0.2 */
+    double restart_necessary;  /* mixed: 0.8 */
+    double restart_artificial; /* mixed: 0.36 */
+    double primal_weight_smoothing; /* mixed: 0.5 */
+    int32_t exact_arithmetic;  /* plain: 1 = the reference kernels' arithmetic (one thread per row/column,
+                                  entry-order sums, no fused multiply-add); results then equal the CPU
+                                  restatement bit for bit.  0 = warp-cooperative SpMV with FMA (default) */
+    int32_t lanes_csr;         /* threads per row of the A x SpMV; 0 = automatic (autotuner or heuristic) */
+    int32_t lanes_csc;         /* threads per column of the A^T y SpMV; 0 = automatic */
+    int32_t heavy_factor;      /* rows/columns longer than heavy_factor * lanes go to whole warps (16) */
+} sih_pdhg_options;
+
+/*
+ * Result of one solve.  The caller owns the arrays; any may be NULL.
+ * Fields mirror what GpuSolver::solve_pdhg writes into sih::model::Solution
+ * (core/src/gpu/gpu_solver.cpp:290-304) plus the fields it leaves empty.
+ */
+typedef struct sih_pdhg_result {
+    double* x;             /* [n]  plain: best checked iterate, as the reference; mixed: returned iterate */
+    double* row_duals;     /* [m]  sign per options.dual_sign */
+    double* slack;         /* [m]  row activity A x */
+    double* reduced_costs; /* [n]  c - A^T y_simplex (original space) */
+    int32_t status;        /* SIH_STATUS_* */
+    int32_t reserved0;
+    int64_t iterations;    /* Solution::simplex_iterations semantics (plain: max_iterations + 1 when not converged) */
+    double primal_objective;
+    double dual_bound;
+    double rel_primal;     /* relative KKT of the returned point, FP64 (docs/gpu_pdhg.md:51-57) */
+    double rel_dual;
+    double rel_gap;
+    double ref_primal;     /* the reference's own termination measures at the last check (plain) */
+    double ref_dual;
+    double time_wall_sec;
+    double time_solver_sec; /* device time of the iteration loop */
+    int64_t restarts;
+    int64_t step_rejections;
+    double final_step;
+    double final_primal_weight;
+} sih_pdhg_result;
+
+/* ---- metadata ----------------------------------------------------------- */
+int sih_pdhg_abi_version(void);
+/* Message of the calling thread's last failed call ("" if none). */
+const char* sih_pdhg_last_error(void);
+void sih_pdhg_config_default(sih_pdhg_config* cfg);
+void sih_pdhg_options_default(sih_pdhg_options* opts);
+
+/* Replaces GpuSolver::is_cuda_available (core/src/gpu/gpu_solver.cpp:42-46).
+ * Returns 1 when a CUDA device is visible, else 0. */
+int sih_pdhg_is_cuda_available(void);
+
+/* Replaces GpuSolver::get_vram_info (core/src/gpu/gpu_solver.cpp:48-58).
+ * On the current device.  Errors: SIH_PDHG_ERR_NO_DEVICE. */
+int sih_pdhg_get_vram_info(uint64_t* total_bytes, uint64_t* free_bytes, uint64_t* used_bytes);
+
+/*
+ * Replaces GpuSolver::solve_pdhg (core/src/gpu/gpu_solver.cpp:60-307).
+ * The reference's FP32 PDHG on the current device: same initial point, step
+ * sizes, iteration, termination test, best-iterate rule and Solution fields,
+ * computed by sm_103a kernels.  Host buffers in, host buffers out.
+ * m == 0 or n == 0 returns OK with status Optimal (gpu_solver.cpp:77-80).
+ * No device: returns SIH_PDHG_ERR_NO_DEVICE (the reference fell back to CPU
+ * simplex, gpu_solver.cpp:66-71; this engine has no CPU fallback).
+ */
+int sih_pdhg_solve(const sih_pdhg_problem* problem, const sih_pdhg_config* config, sih_pdhg_result* result);
+
+/* sih_pdhg_solve with the added options (algorithm choice etc.).  opts may be NULL (defaults). */
+int sih_pdhg_solve_ex(const sih_pdhg_problem* problem, const sih_pdhg_config* config,
+                      const sih_pdhg_options* opts, sih_pdhg_result* result);
+
+/* ---- kernel launchers (device pointers, int32 indices, float values) -----
+ * Same arguments and results as the reference's launchers; the reference
+ * driver binds them at core/src/gpu/gpu_solver.cpp:18-40. */
+
+/* Replaces launch_csr_spmv (core/src/gpu/cuda_pdhg.cu:155-161): y = A x, A in CSR. */
+int sih_pdhg_launch_csr_spmv(int m, const int* d_row_ptr, const int* d_col_ind, const float* d_values,
+                             const float* d_x, float* d_y, void* stream);
+/* Replaces launch_csc_spmv (cuda_pdhg.cu:163-169): z = A^T y, A in CSC. */
+int sih_pdhg_launch_csc_spmv(int n, const int* d_col_ptr, const int* d_row_ind, const float* d_values,
+                             const float* d_y, float* d_z, void* stream);
+/* Replaces launch_primal_update (cuda_pdhg.cu:171-177):
+ * x <- clip(x - tau (c + A^T y), l, u), x_bar <- 2 x_new - x_old. */
+int sih_pdhg_launch_primal_update(int n, const float* d_tau, const float* d_c, const float* d_AT_y,
+                                  const float* d_l, const float* d_u, float* d_x, float* d_x_bar, void* stream);
+/* Replaces launch_dual_update (cuda_pdhg.cu:179-185):
+ * w = A x_bar + y / sigma, y <- sigma (w - clip(w, row_l, row_u)). */
+int sih_pdhg_launch_dual_update(int m, const float* d_sigma, const float* d_A_xbar, const float* d_row_l,
+                                const float* d_row_u, float* d_y, void* stream);
+/* Replaces launch_restart (cuda_pdhg.cu:187-191): x_bar <- x. */
+int sih_pdhg_launch_restart(int n, const float* d_x, float* d_x_bar, void* stream);
+/* Replaces launch_residuals (cuda_pdhg.cu:193-203): per-row bound violation of A x and
+ * per-column |x - clip(x - tau (c + A^T y))| / max(1e-4, tau). */
+int sih_pdhg_launch_residuals(int m, int n, const float* d_Ax, const float* d_row_l, const float* d_row_u,
+                              float* d_row_viols, const float* d_x, const float* d_c, const float* d_AT_y,
+                              const float* d_l, const float* d_u, const float* d_tau, float* d_col_viols,
+                              void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SIH_PDHG_H */

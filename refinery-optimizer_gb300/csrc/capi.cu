@@ -1,0 +1,168 @@
+// C-ABI entry points (include/sih_pdhg.h).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+#include "host.h"
+#include "mixed.h"
+#include "plain.h"
+
+namespace sihg {
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+static bool device_present() {
+    int count = 0;
+    return cudaGetDeviceCount(&count) == cudaSuccess && count > 0;
+}
+
+static void clear_result_scalars(sih_pdhg_result* r) {
+    r->status = SIH_STATUS_UNKNOWN;
+    r->reserved0 = 0;
+    r->iterations = 0;
+    r->primal_objective = r->dual_bound = 0.0;
+    r->rel_primal = r->rel_dual = r->rel_gap = 0.0;
+    r->ref_primal = r->ref_dual = 0.0;
+    r->time_wall_sec = r->time_solver_sec = 0.0;
+    r->restarts = r->step_rejections = 0;
+    r->final_step = r->final_primal_weight = 0.0;
+}
+
+// Fills the vectors and KKT fields of `r` from an FP64 primal/dual pair of
+// the internal (minimization) problem; y is in the PDHG sign.
+void pack_solution(const sih_pdhg_problem* p, const sih_pdhg_options& opts, const std::vector<double>& x,
+                   const std::vector<double>& y, sih_pdhg_result* r) {
+    const int64_t m = p->num_rows, n = p->num_cols;
+    KktReport k = host_kkt(p, x.data(), y.data(), r->slack, r->reduced_costs);
+    double obj = 0.0;
+    bool finite = true;
+    for (int64_t j = 0; j < n; ++j) {
+        obj += p->c[j] * x[j];
+        finite = finite && std::isfinite(x[j]);
+        if (r->x) r->x[j] = x[j];
+    }
+    for (int64_t i = 0; i < m; ++i) {
+        finite = finite && std::isfinite(y[i]);
+        if (r->row_duals) r->row_duals[i] = opts.dual_sign ? -y[i] * p->sense : y[i];
+    }
+    r->primal_objective = obj + p->obj_offset;
+    r->dual_bound = p->sense * k.dual_obj + p->obj_offset;
+    r->rel_primal = k.rel_primal;
+    r->rel_dual = k.rel_dual;
+    r->rel_gap = k.rel_gap;
+    if (!finite) r->status = SIH_STATUS_NUMERICAL_FAILURE;
+}
+
+static int solve_plain(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
+                       sih_pdhg_result* r) {
+    PlainSolver solver;
+    SIHG_TRY(solver.setup(hp, cfg, opts));
+    SIHG_TRY(solver.iterate());
+    std::vector<float> xf, yf;
+    SIHG_TRY(solver.fetch(xf, yf));
+    std::vector<double> x(xf.begin(), xf.end()), y(yf.begin(), yf.end());
+    r->status = solver.converged() ? SIH_STATUS_OPTIMAL : SIH_STATUS_ITERATION_LIMIT;
+    r->iterations = solver.iterations();
+    r->ref_primal = solver.last_norm_p();
+    r->ref_dual = solver.last_norm_d();
+    r->time_solver_sec = solver.loop_seconds();
+    pack_solution(hp.src, opts, x, y, r);
+    return SIH_PDHG_OK;
+}
+
+}  // namespace sihg
+
+using namespace sihg;
+
+extern "C" {
+
+int sih_pdhg_abi_version(void) { return SIH_PDHG_ABI_VERSION; }
+
+const char* sih_pdhg_last_error(void) { return g_last_error.c_str(); }
+
+void sih_pdhg_config_default(sih_pdhg_config* c) {
+    if (!c) return;
+    c->max_iterations = 4000;
+    c->tol_primal = 1e-4f;
+    c->tol_dual = 1e-4f;
+    c->tol_gap = 1e-4f;
+    c->check_frequency = 25;
+    c->step_tau = 0.0f;
+    c->step_sigma = 0.0f;
+    c->enable_restart = 1;
+    c->enable_hybrid_polish = 1;
+}
+
+void sih_pdhg_options_default(sih_pdhg_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->struct_size = (int32_t)sizeof(sih_pdhg_options);
+    o->algorithm = SIH_PDHG_ALGO_PLAIN;
+    o->ruiz_iterations = 10;
+    o->pock_chambolle = 1;
+    o->eval_frequency = 64;
+    o->compensated = 1;
+    o->dual_sign = 0;
+    o->use_graph = 1;
+    o->autotune = 0;
+    o->verbose = 0;
+    o->time_limit_sec = 0.0;
+    o->restart_sufficient = 0.2;
+    o->restart_necessary = 0.8;
+    o->restart_artificial = 0.36;
+    o->primal_weight_smoothing = 0.5;
+    o->exact_arithmetic = 0;
+    o->lanes_csr = 0;
+    o->lanes_csc = 0;
+    o->heavy_factor = 16;
+}
+
+int sih_pdhg_is_cuda_available(void) { return device_present() ? 1 : 0; }
+
+int sih_pdhg_get_vram_info(uint64_t* total_bytes, uint64_t* free_bytes, uint64_t* used_bytes) {
+    if (!device_present()) return fail(SIH_PDHG_ERR_NO_DEVICE, "no CUDA device");
+    size_t f = 0, t = 0;
+    SIHG_CUDA(cudaMemGetInfo(&f, &t));
+    if (total_bytes) *total_bytes = t;
+    if (free_bytes) *free_bytes = f;
+    if (used_bytes) *used_bytes = t - f;
+    return SIH_PDHG_OK;
+}
+
+int sih_pdhg_solve_ex(const sih_pdhg_problem* problem, const sih_pdhg_config* config, const sih_pdhg_options* opts_in,
+                      sih_pdhg_result* result) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!result) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "result is NULL");
+    clear_result_scalars(result);
+    sih_pdhg_options opts;
+    sih_pdhg_options_default(&opts);
+    if (opts_in) {
+        if (opts_in->struct_size != (int32_t)sizeof(sih_pdhg_options))
+            return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "options.struct_size does not match this library");
+        opts = *opts_in;
+    }
+    if (opts.algorithm != SIH_PDHG_ALGO_PLAIN && opts.algorithm != SIH_PDHG_ALGO_MIXED)
+        return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "unknown algorithm");
+    SIHG_TRY(validate_config(config));
+    HostProblem hp;
+    SIHG_TRY(build_host_problem(problem, hp));  // validates sizes, pointers and every index
+    if (!device_present()) return fail(SIH_PDHG_ERR_NO_DEVICE, "no CUDA device (this engine has no CPU fallback)");
+    if (problem->num_rows == 0 || problem->num_cols == 0) {  // gpu_solver.cpp:77-80
+        result->status = SIH_STATUS_OPTIMAL;
+        for (int64_t j = 0; j < problem->num_cols; ++j)
+            if (result->x) result->x[j] = 0.0;
+        return SIH_PDHG_OK;
+    }
+    int rc = opts.algorithm == SIH_PDHG_ALGO_PLAIN ? solve_plain(hp, *config, opts, result)
+                                                   : solve_mixed(hp, *config, opts, result);
+    result->time_wall_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int sih_pdhg_solve(const sih_pdhg_problem* problem, const sih_pdhg_config* config, sih_pdhg_result* result) {
+    return sih_pdhg_solve_ex(problem, config, nullptr, result);
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+// Shared helpers of the sm_103a PDHG engine: error plumbing, device memory
+// RAII, warp/block reductions, compensated (two-sum) arithmetic.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sih_pdhg.h"
+
+namespace sihg {
+
+// ---------------------------------------------------------------- errors
+void set_last_error(const std::string& msg);
+
+struct Status {
+    int code = SIH_PDHG_OK;
+    bool ok() const { return code == SIH_PDHG_OK; }
+};
+
+inline int fail(int code, const std::string& msg) {
+    set_last_error(msg);
+    return code;
+}
+
+inline int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    return fail(e == cudaErrorMemoryAllocation ? SIH_PDHG_ERR_OUT_OF_MEMORY : SIH_PDHG_ERR_CUDA, buf);
+}
+
+#define SIHG_CUDA(call)                                                   \
+    do {                                                                  \
+        cudaError_t e_ = (call);                                          \
+        if (e_ != cudaSuccess) return ::sihg::cuda_fail(e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define SIHG_LAUNCH_CHECK()                                               \
+    do {                                                                  \
+        cudaError_t e_ = cudaGetLastError();                              \
+        if (e_ != cudaSuccess) return ::sihg::cuda_fail(e_, "kernel launch", __FILE__, __LINE__); \
+    } while (0)
+
+#define SIHG_TRY(expr)                   \
+    do {                                 \
+        int rc_ = (expr);                \
+        if (rc_ != SIH_PDHG_OK) return rc_; \
+    } while (0)
+
+// ---------------------------------------------------------------- device memory
+// Owning device allocation (cudaMalloc / cudaFree), movable, never copied.
+class DevMem {
+  public:
+    DevMem() = default;
+    DevMem(const DevMem&) = delete;
+    DevMem& operator=(const DevMem&) = delete;
+    DevMem(DevMem&& o) noexcept : p_(o.p_), bytes_(o.bytes_) { o.p_ = nullptr; o.bytes_ = 0; }
+    DevMem& operator=(DevMem&& o) noexcept {
+        if (this != &o) { release(); p_ = o.p_; bytes_ = o.bytes_; o.p_ = nullptr; o.bytes_ = 0; }
+        return *this;
+    }
+    ~DevMem() { release(); }
+    int alloc(size_t bytes) {
+        release();
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMalloc(&p_, bytes);
+        if (e != cudaSuccess) { p_ = nullptr; return cuda_fail(e, "cudaMalloc", __FILE__, __LINE__); }
+        bytes_ = bytes;
+        return SIH_PDHG_OK;
+    }
+    void release() {
+        if (p_) cudaFree(p_);
+        p_ = nullptr;
+        bytes_ = 0;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p_); }
+    size_t bytes() const { return bytes_; }
+
+  private:
+    void* p_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+// ---------------------------------------------------------------- device helpers
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(FULL_MASK, v, o));
+    return v;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_maxd(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL_MASK, v, o));
+    return v;
+}
+
+// Block-wide max of non-negative floats, result valid in thread 0.
+// `smem` must hold blockDim.x / 32 floats.
+__device__ __forceinline__ float block_max_nonneg(float v, float* smem) {
+    v = warp_max(v);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) smem[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? smem[lane] : 0.0f;
+        v = warp_max(v);
+    }
+    __syncthreads();
+    return v;
+}
+
+// Knuth's two-sum: s + e == a + b exactly (round-to-nearest).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Two-product via fused multiply-add: p + e == a * b exactly.
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+
+}  // namespace sihg

@@ -1,0 +1,84 @@
+// Host-side problem preparation: validation of the C-ABI problem, FP64 -> FP32
+// conversion into the engine's packed layout, and the FP64 KKT certificate.
+#pragma once
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "sih_pdhg.h"
+
+namespace sihg {
+
+// One nonzero in the packed layout: {index, value}.  Same bytes as the int2
+// {index, __float_as_int(value)} the kernels load.
+struct Pair {
+    int32_t idx;
+    float val;
+};
+
+// The engine's host copy of one LP.
+struct HostProblem {
+    int m = 0, n = 0, nnz = 0;
+    std::vector<int> csc_ptr;   // [n + 1]
+    std::vector<Pair> csc;      // [nnz] row index, value (columns' entries)
+    std::vector<int> csr_ptr;   // [m + 1]
+    std::vector<Pair> csr;      // [nnz] column index, value (rows' entries, columns ascending)
+    std::vector<float> c, l, u; // [n] FP32 casts (objective already multiplied by sense)
+    std::vector<float> rl, ru;  // [m]
+    const sih_pdhg_problem* src = nullptr; // original FP64 data (not owned)
+    int sense = 1;
+};
+
+// Validates `p` and fills `hp` (multithreaded conversion).  Errors:
+// SIH_PDHG_ERR_INVALID_ARGUMENT (with a message) or SIH_PDHG_ERR_UNSUPPORTED.
+int build_host_problem(const sih_pdhg_problem* p, HostProblem& hp);
+
+// Validation only (used by entry points before any device work).
+int validate_problem(const sih_pdhg_problem* p);
+int validate_config(const sih_pdhg_config* c);
+
+struct KktReport {
+    double rel_primal, rel_dual, rel_gap, primal_obj, dual_obj;
+};
+
+// FP64 KKT of (x, y_pdhg) for the ORIGINAL problem p (sense applied):
+// primal residual of A x against the row bounds, dual residual of the reduced
+// cost lambda = sense*c + A^T y that no finite bound can carry, duality gap;
+// relative measures of docs/gpu_pdhg.md:51-57.  Optionally writes slack = A x
+// and reduced_costs = sense * lambda (simplex convention, original sense).
+KktReport host_kkt(const sih_pdhg_problem* p, const double* x, const double* y_pdhg, double* slack,
+                   double* reduced_costs);
+
+// Runs f(begin, end) over [0, count) split across hardware threads.
+template <class F>
+void parallel_for(int64_t count, F&& f);
+
+bool bound_is_finite(double v);
+int hardware_threads();
+
+}  // namespace sihg
+
+#include <thread>
+
+namespace sihg {
+template <class F>
+void parallel_for(int64_t count, F&& f) {
+    const int64_t min_chunk = 1 << 16;
+    int t = hardware_threads();
+    if (count < min_chunk * 2 || t <= 1) {
+        f((int64_t)0, count);
+        return;
+    }
+    int64_t chunks = (count + min_chunk - 1) / min_chunk;
+    if (chunks < t) t = (int)chunks;
+    std::vector<std::thread> pool;
+    pool.reserve(t);
+    for (int i = 0; i < t; ++i) {
+        const int64_t b = count * i / t, e = count * (i + 1) / t;
+        pool.emplace_back([&f, b, e] { f(b, e); });
+    }
+    for (auto& th : pool) th.join();
+}
+}  // namespace sihg

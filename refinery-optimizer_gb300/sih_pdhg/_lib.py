@@ -1,0 +1,122 @@
+"""ctypes binding of the engine's C ABI (include/sih_pdhg.h).
+
+The library is ``refinery-optimizer_gb300/_build/libsih_pdhg.so`` built by
+``refinery-optimizer_gb300/build.py``.  There is no fallback: if the library is
+missing, loading raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .config import GpuPdhgConfig
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "_build", "libsih_pdhg.so")
+
+OK = 0
+ERR_NAMES = {1: "invalid argument", 2: "no CUDA device", 3: "CUDA error", 4: "out of memory", 5: "unsupported"}
+
+ALGO_PLAIN = 0
+ALGO_MIXED = 1
+
+
+class SihPdhgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sih_pdhg error {code} ({ERR_NAMES.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class CProblem(C.Structure):
+    _fields_ = [("num_rows", C.c_int64), ("num_cols", C.c_int64), ("num_nonzeros", C.c_int64),
+                ("csc_col_ptr", C.c_void_p), ("csc_row_ind", C.c_void_p), ("csc_values", C.c_void_p),
+                ("csr_row_ptr", C.c_void_p), ("csr_col_ind", C.c_void_p), ("csr_values", C.c_void_p),
+                ("c", C.c_void_p), ("col_lower", C.c_void_p), ("col_upper", C.c_void_p),
+                ("row_lower", C.c_void_p), ("row_upper", C.c_void_p), ("sense", C.c_int32),
+                ("obj_offset", C.c_double)]
+
+
+class COptions(C.Structure):
+    _fields_ = [("struct_size", C.c_int32), ("algorithm", C.c_int32), ("ruiz_iterations", C.c_int32),
+                ("pock_chambolle", C.c_int32), ("eval_frequency", C.c_int32), ("compensated", C.c_int32),
+                ("dual_sign", C.c_int32), ("use_graph", C.c_int32), ("autotune", C.c_int32),
+                ("verbose", C.c_int32), ("time_limit_sec", C.c_double), ("restart_sufficient", C.c_double),
+                ("restart_necessary", C.c_double), ("restart_artificial", C.c_double),
+                ("primal_weight_smoothing", C.c_double), ("exact_arithmetic", C.c_int32),
+                ("lanes_csr", C.c_int32), ("lanes_csc", C.c_int32), ("heavy_factor", C.c_int32)]
+
+
+class CResult(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("row_duals", C.c_void_p), ("slack", C.c_void_p),
+                ("reduced_costs", C.c_void_p), ("status", C.c_int32), ("reserved0", C.c_int32),
+                ("iterations", C.c_int64), ("primal_objective", C.c_double), ("dual_bound", C.c_double),
+                ("rel_primal", C.c_double), ("rel_dual", C.c_double), ("rel_gap", C.c_double),
+                ("ref_primal", C.c_double), ("ref_dual", C.c_double), ("time_wall_sec", C.c_double),
+                ("time_solver_sec", C.c_double), ("restarts", C.c_int64), ("step_rejections", C.c_int64),
+                ("final_step", C.c_double), ("final_primal_weight", C.c_double)]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the engine library (raises RuntimeError if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python refinery-optimizer_gb300/build.py` "
+                           "(the engine has no CPU fallback)")
+    lib = C.CDLL(LIB_PATH)
+    vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
+    lib.sih_pdhg_abi_version.restype = i32
+    lib.sih_pdhg_last_error.restype = C.c_char_p
+    lib.sih_pdhg_is_cuda_available.restype = i32
+    lib.sih_pdhg_get_vram_info.argtypes = [C.POINTER(C.c_uint64)] * 3
+    lib.sih_pdhg_solve.argtypes = [C.POINTER(CProblem), C.POINTER(GpuPdhgConfig), C.POINTER(CResult)]
+    lib.sih_pdhg_solve_ex.argtypes = [C.POINTER(CProblem), C.POINTER(GpuPdhgConfig), C.POINTER(COptions),
+                                      C.POINTER(CResult)]
+    lib.sih_pdhg_options_default.argtypes = [C.POINTER(COptions)]
+    lib.sih_pdhg_config_default.argtypes = [C.POINTER(GpuPdhgConfig)]
+    lib.sih_pdhg_launch_csr_spmv.argtypes = [i32, vp, vp, vp, vp, vp, vp]
+    lib.sih_pdhg_launch_csc_spmv.argtypes = [i32, vp, vp, vp, vp, vp, vp]
+    lib.sih_pdhg_launch_primal_update.argtypes = [i32, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.sih_pdhg_launch_dual_update.argtypes = [i32, vp, vp, vp, vp, vp, vp]
+    lib.sih_pdhg_launch_restart.argtypes = [i32, vp, vp, vp]
+    lib.sih_pdhg_launch_residuals.argtypes = [i32, i32] + [vp] * 12
+    for name in dir(lib):
+        pass
+    _lib = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != OK:
+        raise SihPdhgError(rc, load().sih_pdhg_last_error().decode(errors="replace"))
+
+
+def default_options(**kw) -> COptions:
+    o = COptions()
+    load().sih_pdhg_options_default(C.byref(o))
+    for k, v in kw.items():
+        if not any(k == f[0] for f in COptions._fields_):
+            raise AttributeError(f"unknown option {k!r}")
+        setattr(o, k, v)
+    return o
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def c_problem(problem):
+    """CProblem view of a sih_pdhg.Problem (keeps the arrays alive in `keep`)."""
+    A = problem.A
+    keep = [np.ascontiguousarray(a) for a in (A.csc_col_ptr(), A.csc_row_ind(), A.csc_values(), A.csr_row_ptr(),
+                                              A.csr_col_ind(), A.csr_values(), problem.c, problem.col_lower,
+                                              problem.col_upper, problem.row_lower, problem.row_upper)]
+    cp = CProblem(problem.num_rows(), problem.num_cols(), problem.num_nonzeros(), *[_ptr(a) for a in keep],
+                  int(problem.sense), float(problem.obj_offset))
+    return cp, keep

@@ -1,0 +1,131 @@
+"""The C ABI library loads, exports every declared symbol, and its structs
+have the layout the Python binding (and the reference's config struct) use."""
+import ctypes as C
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+HEADER_DIR = os.path.join(REPO, "include")
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(HEADER_DIR)):
+        if h.endswith(".h"):
+            text = open(os.path.join(HEADER_DIR, h)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names += re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(sih_pdhg_[a-z_0-9]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("sih_pdhg_solve", "sih_pdhg_solve_ex", "sih_pdhg_is_cuda_available", "sih_pdhg_get_vram_info",
+                 "sih_pdhg_launch_csr_spmv", "sih_pdhg_launch_csc_spmv", "sih_pdhg_launch_primal_update",
+                 "sih_pdhg_launch_dual_update", "sih_pdhg_launch_restart", "sih_pdhg_launch_residuals"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    from sih_pdhg import _lib
+
+    lib = _lib.load()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """sizeof/offsetof from a C compile of the header equal the ctypes layouts."""
+    from sih_pdhg import _lib
+    from sih_pdhg.config import GpuPdhgConfig
+
+    src = tmp_path / "sizes.c"
+    fields = {"sih_pdhg_config": GpuPdhgConfig, "sih_pdhg_options": _lib.COptions,
+              "sih_pdhg_result": _lib.CResult, "sih_pdhg_problem": _lib.CProblem}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sih_pdhg.h"', "int main(void){"]
+    for sname, cls in fields.items():
+        lines.append(f'printf("{sname} %zu\\n", sizeof({sname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{sname}.{f} %zu\\n", offsetof({sname}, {f}));')
+    lines.append("return 0;}")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sizes"
+    subprocess.check_call(["gcc", "-I", HEADER_DIR, str(src), "-o", str(exe)])
+    out = dict(l.rsplit(" ", 1) for l in subprocess.check_output([str(exe)]).decode().split("\n") if l)
+    for sname, cls in fields.items():
+        assert int(out[sname]) == C.sizeof(cls), sname
+        for f, _ in cls._fields_:
+            assert int(out[f"{sname}.{f}"]) == getattr(cls, f).offset, f"{sname}.{f}"
+
+
+def test_config_defaults_match_reference():
+    """GpuPdhgConfig defaults of core/include/sih/gpu/gpu_solver.hpp:12-22."""
+    from sih_pdhg import _lib
+    from sih_pdhg.config import GpuPdhgConfig
+
+    c = GpuPdhgConfig()
+    _lib.load().sih_pdhg_config_default(C.byref(c))
+    assert (c.max_iterations, c.check_frequency, c.enable_restart, c.enable_hybrid_polish) == (4000, 25, True, True)
+    assert c.tol_primal == pytest.approx(1e-4) and c.tol_dual == pytest.approx(1e-4) and c.tol_gap == pytest.approx(1e-4)
+    assert c.step_tau == 0.0 and c.step_sigma == 0.0
+    py = GpuPdhgConfig()
+    assert bytes(py) == bytes(c)
+
+
+def test_invalid_arguments_rejected_before_device_work():
+    """Malformed input returns SIH_PDHG_ERR_INVALID_ARGUMENT with a message, GPU or not."""
+    import sih_pdhg
+    from sih_pdhg import _lib
+    from sih_pdhg.generators import small_random_lp
+
+    p = small_random_lp(20, 40, 3, 0)
+    bad = small_random_lp(20, 40, 3, 0)
+    bad.A._ri = bad.A._ri.copy()
+    bad.A._ri[5] = 10_000
+    with pytest.raises(sih_pdhg.SihPdhgError) as e:
+        sih_pdhg.solve_gpu_pdhg(bad)
+    assert e.value.code == 1 and "csc_row_ind" in str(e.value)
+    with pytest.raises(sih_pdhg.SihPdhgError) as e:
+        sih_pdhg.solve_gpu_pdhg(p, sih_pdhg.GpuPdhgConfig(check_frequency=0))
+    assert e.value.code == 1
+    with pytest.raises(sih_pdhg.SihPdhgError) as e:
+        sih_pdhg.GpuSolver.solve_ex(p, None, algorithm=7)
+    assert e.value.code == 1
+
+
+def test_no_device_is_an_error_not_a_fallback():
+    import sih_pdhg
+    from sih_pdhg.generators import small_random_lp
+
+    if sih_pdhg.GpuSolver.is_cuda_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(sih_pdhg.SihPdhgError) as e:
+        sih_pdhg.solve_gpu_pdhg(small_random_lp(20, 40, 3, 0))
+    assert e.value.code == 2
+
+
+def test_generators_are_deterministic():
+    from sih_pdhg.generators import small_random_lp, zipf_lp
+
+    a, b = small_random_lp(300, 700, 5, 3), small_random_lp(300, 700, 5, 3)
+    np.testing.assert_array_equal(a.A.csc_row_ind(), b.A.csc_row_ind())
+    np.testing.assert_array_equal(a.c, b.c)
+    z = zipf_lp(5000, 10000, 120000, seed=1)
+    cnt = np.diff(z.A.csc_col_ptr())
+    assert z.num_nonzeros() == 120000 and cnt.min() >= 2 and cnt.max() <= 2000
+    # rows distinct within a column and sorted
+    for j in range(0, 10000, 997):
+        r = z.A.csc_row_ind()[z.A.csc_col_ptr()[j]:z.A.csc_col_ptr()[j + 1]]
+        assert np.all(np.diff(r) > 0)
+    # CSR holds the same entries
+    x = np.random.default_rng(0).standard_normal(10000)
+    dense_ax = z.A.mat_vec(x)
+    cols = np.repeat(np.arange(10000), cnt)
+    ref = np.bincount(z.A.csc_row_ind(), weights=z.A.csc_values() * x[cols], minlength=5000)
+    np.testing.assert_allclose(dense_ax, ref, rtol=1e-12, atol=1e-12)
