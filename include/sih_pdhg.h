@@ -124,6 +124,7 @@ typedef struct sih_pdhg_options {
     int32_t lanes_csr;         /* threads per row of the A x SpMV; 0 = automatic (autotuner or heuristic) */
     int32_t lanes_csc;         /* threads per column of the A^T y SpMV; 0 = automatic */
     int32_t heavy_factor;      /* rows/columns longer than heavy_factor * lanes go to whole warps (16) */
+    int32_t tile_nnz;          /* mixed: nonzeros per shared-memory tile of the SpMV (0 = 2048) */
 } sih_pdhg_options;
 
 /*

@@ -17,11 +17,12 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (-ffp-contract=off keeps float ops unfused)."""
-    src = os.path.join(HERE, "pdhg_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, "pdhg_oracle.c"), os.path.join(HERE, "pdlp_oracle.c")]
+    newest = max(os.path.getmtime(s) for s in srcs + [os.path.abspath(__file__)])
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
         os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
         subprocess.check_call(["gcc", "-O3", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-                               src, "-o", LIB_PATH, "-lm"])
+                               *srcs, "-o", LIB_PATH, "-lm"])
     return LIB_PATH
 
 
@@ -131,3 +132,38 @@ def dual_update_f32(sigma, axbar, rl, ru, y):
     lib().oracle_dual_update_f32(C.c_int(y.shape[0]), _p(sigma, C.c_float), _p(axbar, C.c_float),
                                  _p(rl, C.c_float), _p(ru, C.c_float), _p(y, C.c_float))
     return y
+
+
+class PdlpOpts(C.Structure):
+    _fields_ = [("ruiz_iterations", C.c_int32), ("pock_chambolle", C.c_int32), ("eval_frequency", C.c_int32),
+                ("enable_restart", C.c_int32), ("max_attempts", C.c_int64), ("tol_p", C.c_double),
+                ("tol_d", C.c_double), ("tol_g", C.c_double), ("beta_suff", C.c_double), ("beta_nec", C.c_double),
+                ("beta_art", C.c_double), ("weight_smoothing", C.c_double), ("fp32_bits", C.c_int32)]
+
+
+class PdlpInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("out_sel", C.c_int32), ("attempts", C.c_int64), ("steps", C.c_int64),
+                ("rejections", C.c_int64), ("restarts", C.c_int64), ("evals", C.c_int64), ("eta", C.c_double),
+                ("omega", C.c_double), ("rel_p", C.c_double), ("rel_d", C.c_double), ("rel_g", C.c_double),
+                ("pobj", C.c_double), ("dobj", C.c_double)]
+
+
+def pdlp_solve(problem, max_attempts=100000, tol=1e-4, tol_p=None, tol_d=None, tol_g=None, eval_frequency=64,
+               ruiz_iterations=10, pock_chambolle=1, enable_restart=1, fp32_bits=0):
+    """FP64 restarted adaptive PDHG (the algorithm of the mixed CUDA path).
+    Returns (x, y_pdhg, info dict); a maximization problem is solved as min -c."""
+    A = problem.A
+    m, n = problem.num_rows(), problem.num_cols()
+    o = PdlpOpts(ruiz_iterations, pock_chambolle, eval_frequency, enable_restart, max_attempts,
+                 tol if tol_p is None else tol_p, tol if tol_d is None else tol_d, tol if tol_g is None else tol_g,
+                 0.2, 0.8, 0.36, 0.5, fp32_bits)
+    c = np.ascontiguousarray(problem.c * (1 if int(problem.sense) == 1 else -1), dtype=np.float64)
+    x = np.zeros(n)
+    y = np.zeros(m)
+    info = PdlpInfo()
+    lib().pdlp_oracle_solve(C.c_int64(m), C.c_int64(n), _p(A.csc_col_ptr(), C.c_int64), _p(A.csc_row_ind(), C.c_int64),
+                            _p(A.csc_values(), C.c_double), _p(c, C.c_double), _p(problem.col_lower, C.c_double),
+                            _p(problem.col_upper, C.c_double), _p(problem.row_lower, C.c_double),
+                            _p(problem.row_upper, C.c_double), C.byref(o), _p(x, C.c_double), _p(y, C.c_double),
+                            C.byref(info))
+    return x, y, {k: getattr(info, k) for k, _ in PdlpInfo._fields_}

@@ -135,4 +135,44 @@ __device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
     e = __fmaf_rn(a, b, -p);
 }
 
+// Compensated FP32 accumulator (Neumaier summation built on two-sum): the
+// running value is s + c with an error of about eps^2 relative to the sum of
+// magnitudes.  Per-element reductions use it so that FP64 (a slow pipe on this
+// part) is only touched once per thread at the block reduction.
+struct Acc {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        float t, e;
+        two_sum(s, v, t, e);
+        s = t;
+        c = __fadd_rn(c, e);
+    }
+    // adds a * b exactly (two-product)
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        float p, e;
+        two_prod(a, b, p, e);
+        add(p);
+        c = __fadd_rn(c, e);
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+    __device__ __forceinline__ void reset() { s = c = 0.f; }
+};
+
+// Float-float number hi + lo (about 48 significant bits): the running averages.
+__device__ __forceinline__ float2 ff_axpy(float2 acc, float w, float x) {
+    // acc + w * (x - acc), evaluated in float-float arithmetic
+    float d_hi, d_lo;
+    two_sum(x, -acc.x, d_hi, d_lo);
+    d_lo = __fsub_rn(d_lo, acc.y);
+    const float d = __fadd_rn(d_hi, d_lo);
+    float p, pe;
+    two_prod(w, d, p, pe);
+    float s, se;
+    two_sum(acc.x, p, s, se);
+    const float lo = __fadd_rn(__fadd_rn(acc.y, se), pe);
+    float hi2, lo2;
+    two_sum(s, lo, hi2, lo2);
+    return make_float2(hi2, lo2);
+}
+
 }  // namespace sihg

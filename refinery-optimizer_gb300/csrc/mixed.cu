@@ -1,7 +1,1046 @@
+// Mixed-precision restarted adaptive PDHG on the device, for one LP or a batch
+// of independent LPs (block-diagonal concatenation, per-instance state).
+//
+// Algorithm (the reference specifies it in docs/gpu_pdhg.md:29-57; the code
+// path it ships does not have it, so the adaptive pieces follow the published
+// PDLP method: Applegate et al., "Practical large-scale linear programming
+// using primal-dual hybrid gradient", NeurIPS 2021, and its GPU form cuPDLP,
+// Lu & Yang 2023):
+//   scaling   Ruiz equilibration (inf-norm, `ruiz_iterations` passes) then one
+//             Pock-Chambolle pass (alpha = 1) on the device;
+//   step      tau = eta / omega, sigma = eta * omega; eta adapted every step:
+//             eta_bar = (omega |dx|^2 + |dy|^2 / omega) / (2 |dx' K' dy|),
+//             accept when eta <= eta_bar, next
+//             eta = min((1 - (k+1)^-0.3) eta_bar, (1 + (k+1)^-0.6) eta);
+//   restart   every `eval_frequency` steps: KKT of the current and of the
+//             step-weighted average iterate; restart to the better one on
+//             sufficient (0.2), necessary-without-progress (0.8) or artificial
+//             (0.36 of all steps) decay of the weighted KKT error;
+//   weight    at a restart omega <- exp(0.5 log(|dy|/|dx|) + 0.5 log omega)
+//             from the distances moved since the previous restart;
+//   stop      relative KKT of docs/gpu_pdhg.md:51-57 (inf-norms, original
+//             space) of the current or average point <= tolerances.
+// Precision: matrix, iterates and SpMV products in FP32; every reduction
+// (norms, objectives, gap, step-size terms, primal weight) in FP64; the
+// evaluation SpMVs use compensated Dot2 sums near the tolerance.
+//
+// PDHG sign: y is the reference's y_pdhg (= -simplex dual), the dual step is
+// the reference's y <- sigma (w - clip(w, rl, ru)), w = K xbar + y / sigma
+// (core/src/gpu/cuda_pdhg.cu:82-103), with K xbar = 2 K x' - K x by linearity.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
 #include "mixed.h"
+#include "warp.cuh"
 
 namespace sihg {
-int solve_mixed(const HostProblem&, const sih_pdhg_config&, const sih_pdhg_options&, sih_pdhg_result*) {
-    return fail(SIH_PDHG_ERR_UNSUPPORTED, "mixed algorithm not built yet");
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ float* pick(float* a, float* b, int sel) { return sel ? b : a; }
+__device__ __forceinline__ bool fin(float v) { return !isinf(v); }
+
+// a - (s + e) for a float a and a float-float s + e, without losing the low part
+__device__ __forceinline__ float diff_ff(float a, float s, float e) {
+    float h, l;
+    two_sum(a, -s, h, l);
+    return __fadd_rn(h, __fsub_rn(l, e));
 }
+
+// Bound violation of the float-float row activity s + e (0 inside [rl, ru]).
+__device__ __forceinline__ float row_violation(float s, float e, float rl, float ru) {
+    float v = 0.f;
+    if (fin(rl)) v = fmaxf(v, diff_ff(rl, s, e));
+    if (fin(ru)) v = fmaxf(v, -diff_ff(ru, s, e));
+    return v;
+}
+
+// dual objective contribution of a row (scaling invariant), PDHG sign y
+__device__ __forceinline__ void row_dual_term(Acc& acc, float y, float rl, float ru) {
+    if (y < 0.f && fin(rl)) acc.add_prod(-y, rl);
+    if (y > 0.f && fin(ru)) acc.add_prod(-y, ru);
+}
+
+// ---------------------------------------------------------------- step kernels
+// Elementwise part of a step.  Columns: pending float-float average update of
+// x, then x' = clip(x - tau (c + K^T y), l, u).  Rows: pending average update of y.
+__global__ void __launch_bounds__(kThreads) k_step_primal(Side cols, Side rows, Vecs V, Inst* __restrict__ st) {
+    for_each_segment_both(cols, rows, st, [&](bool is_col, const Inst& S, int r) {
+        const int cur = S.cur;
+        const bool avg = S.avg_pending;
+        const float w = (float)S.avg_w;
+        if (is_col) {
+            const float xj = pick(V.x0, V.x1, cur)[r];
+            if (avg) V.x_acc[r] = ff_axpy(V.x_acc[r], w, xj);
+            const float tau = (float)(S.eta / S.omega);
+            const float v = fmaf(-tau, V.c[r] + pick(V.kty0, V.kty1, cur)[r], xj);
+            pick(V.x0, V.x1, cur ^ 1)[r] = fminf(fmaxf(v, V.l[r]), V.u[r]);
+        } else if (avg) {
+            V.y_acc[r] = ff_axpy(V.y_acc[r], w, pick(V.y0, V.y1, cur)[r]);
+        }
+    });
+}
+
+// Row epilogue of a step: K x' arrives as the dot product; dual update with
+// K xbar = 2 K x' - K x (cuda_pdhg.cu:82-103 form, PDHG sign).
+struct DualStepEpi {
+    Vecs V;
+    const float *xg, *kx, *y;
+    float *kxn, *yn;
+    float sigma;
+    Acc dy2;
+    struct Pre { float kx, y, rl, ru; };
+    __device__ Pre pre(int i) const { return Pre{kx[i], y[i], V.rl[i], V.ru[i]}; }
+    __device__ void begin(const Inst& S) {
+        xg = pick(V.x0, V.x1, S.cur ^ 1);
+        kx = pick(V.kx0, V.kx1, S.cur);
+        y = pick(V.y0, V.y1, S.cur);
+        kxn = pick(V.kx0, V.kx1, S.cur ^ 1);
+        yn = pick(V.y0, V.y1, S.cur ^ 1);
+        sigma = (float)(S.eta * S.omega);
+    }
+    __device__ const float* gather(int) const { return xg; }
+    __device__ void apply(int i, const SegDot<1>& d, const Pre& p) {
+        const float kxp = d.f(0);  // hi + lo when compensated
+        const float wv = (2.0f * kxp - p.kx) + p.y / sigma;
+        const float yv = sigma * (wv - fminf(fmaxf(wv, p.rl), p.ru));
+        kxn[i] = kxp;
+        yn[i] = yv;
+        const float dy = yv - p.y;
+        dy2.add(dy * dy);
+    }
+    __device__ void values(double (&q)[1]) {
+        q[0] = dy2.value();
+        dy2.reset();
+    }
+    __device__ void finish(Inst& S, const double* tot) { S.dy2 = tot[0]; }
+};
+
+__global__ void __launch_bounds__(kThreads, 6) k_step_dual(Side rows, Vecs V, Inst* __restrict__ st) {
+    DualStepEpi epi{V};
+    block_engine<1, true, 1>(rows, st, epi, 0u);
+}
+
+// Step-size controller of one instance (PDLP adaptive step), one thread.
+__device__ void step_controller(Inst& S, double dx2, double inter) {
+    const double om = S.omega;
+    const double movement = om * dx2 + S.dy2 / om;
+    const double ai = fabs(inter);
+    const double eta_bar = ai > 0.0 ? movement / (2.0 * ai) : INFINITY;
+    // PDLP counts iterations from 1: the base (k + 1) is at least 2
+    const double k = (double)(S.attempts + 2);
+    const double eta = S.eta;
+    const double grow = (1.0 + pow(k, -0.6)) * eta;
+    const double eta_next = isinf(eta_bar) ? grow : fmin((1.0 - pow(k, -0.3)) * eta_bar, grow);
+    S.attempts += 1;
+    if (!(movement == movement) || !(inter == inter)) {  // NaN: stop as a numerical failure
+        S.done = 3;
+        return;
+    }
+    if (eta <= eta_bar) {
+        S.cur ^= 1;
+        S.steps += 1;
+        S.since_restart += 1;
+        S.W += eta;
+        S.avg_w = eta / S.W;
+        S.avg_pending = 1;
+    } else {
+        S.rejections += 1;
+        S.avg_pending = 0;
+    }
+    S.eta = eta_next;
+}
+
+// Column epilogue of a step: K^T y' as the dot product; interaction and
+// movement terms of the adaptive step.  The warp completing an instance runs
+// its step-size controller.
+struct KtyStepEpi {
+    Vecs V;
+    const float *yg, *x, *xn, *kty;
+    float* ktyn;
+    Acc inter, dx2;
+    struct Pre { float x, xn, kty; };
+    __device__ Pre pre(int j) const { return Pre{x[j], xn[j], kty[j]}; }
+    __device__ void begin(const Inst& S) {
+        yg = pick(V.y0, V.y1, S.cur ^ 1);
+        x = pick(V.x0, V.x1, S.cur);
+        xn = pick(V.x0, V.x1, S.cur ^ 1);
+        kty = pick(V.kty0, V.kty1, S.cur);
+        ktyn = pick(V.kty0, V.kty1, S.cur ^ 1);
+    }
+    __device__ const float* gather(int) const { return yg; }
+    __device__ void apply(int j, const SegDot<1>& d, const Pre& p) {
+        const float k = d.f(0);
+        ktyn[j] = k;
+        const float dx = p.xn - p.x;
+        inter.add(dx * (k - p.kty));
+        dx2.add(dx * dx);
+    }
+    __device__ void values(double (&q)[2]) {
+        q[0] = inter.value();
+        q[1] = dx2.value();
+        inter.reset();
+        dx2.reset();
+    }
+    __device__ void finish(Inst& S, const double* tot) { step_controller(S, tot[1], tot[0]); }
+};
+
+__global__ void __launch_bounds__(kThreads, 6) k_step_kty(Side cols, Vecs V, Inst* __restrict__ st) {
+    KtyStepEpi epi{V};
+    block_engine<1, true, 2>(cols, st, epi, 0u);
+}
+
+// ---------------------------------------------------------------- evaluation kernels
+// Before an evaluation: applies a pending average update and refreshes the
+// FP32 copies x_avg, y_avg that the evaluation gathers.
+__global__ void __launch_bounds__(kThreads) k_flush_avg(Side cols, Side rows, Vecs V, Inst* __restrict__ st) {
+    for_each_segment_both(cols, rows, st, [&](bool is_col, const Inst& S, int r) {
+        const bool avg = S.avg_pending;
+        const float w = (float)S.avg_w;
+        if (is_col) {
+            float2 a = V.x_acc[r];
+            if (avg) V.x_acc[r] = a = ff_axpy(a, w, pick(V.x0, V.x1, S.cur)[r]);
+            V.x_avg[r] = __fadd_rn(a.x, a.y);
+        } else {
+            float2 a = V.y_acc[r];
+            if (avg) V.y_acc[r] = a = ff_axpy(a, w, pick(V.y0, V.y1, S.cur)[r]);
+            V.y_avg[r] = __fadd_rn(a.x, a.y);
+        }
+    });
+}
+
+// Row evaluation of both candidates (0 = current, 1 = average): primal
+// residual of K x_c against the row bounds (scaled 2-norm^2 and original
+// inf-norm), row part of the dual objective, |y_c - y_last|^2.
+struct EvalRowsEpi {
+    Vecs V;
+    const float *xg[2], *yc;
+    Acc p2[2], dterm[2], dyl2[2];
+    float pinf[2];
+    struct Pre { float rl, ru, dr, yc, ya, yl; };
+    __device__ Pre pre(int i) const { return Pre{V.rl[i], V.ru[i], V.drow[i], yc[i], V.y_avg[i], V.y_last[i]}; }
+    __device__ void begin(const Inst& S) {
+        xg[0] = pick(V.x0, V.x1, S.cur);
+        xg[1] = V.x_avg;
+        yc = pick(V.y0, V.y1, S.cur);
+    }
+    __device__ const float* gather(int v) const { return xg[v]; }
+    __device__ void apply(int i, const SegDot<2>& d, const Pre& p) {
+        V.kx_eval[i] = d.f(1);
+        const float yv[2] = {p.yc, p.ya};
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const float res = row_violation(d.s[c], d.e[c], p.rl, p.ru);
+            p2[c].add(res * res);
+            pinf[c] = fmaxf(pinf[c], res / p.dr);
+            row_dual_term(dterm[c], yv[c], p.rl, p.ru);
+            const float dy = yv[c] - p.yl;
+            dyl2[c].add(dy * dy);
+        }
+    }
+    __device__ void values(double (&q)[8]) {
+        const double v[8] = {p2[0].value(),    p2[1].value(),    (double)pinf[0], (double)pinf[1],
+                             dterm[0].value(), dterm[1].value(), dyl2[0].value(), dyl2[1].value()};
+        for (int k = 0; k < 8; ++k) q[k] = v[k];
+        for (int c = 0; c < 2; ++c) {
+            p2[c].reset();
+            dterm[c].reset();
+            dyl2[c].reset();
+            pinf[c] = 0.f;
+        }
+    }
+    __device__ void finish(Inst& S, const double* tot) {
+        for (int k = 0; k < 8; ++k) S.row_eval[k] = tot[k];
+    }
+};
+
+__global__ void __launch_bounds__(kThreads) k_eval_rows(Side rows, Vecs V, Inst* __restrict__ st) {
+    EvalRowsEpi epi{V};
+    block_engine<2, true, 8>(rows, st, epi, 0x0Cu);
+}
+
+// Restart / termination controller of one instance after an evaluation.
+__device__ void eval_controller(Inst& S, const double* cq, unsigned* done_count) {
+    const double* rq = S.row_eval;
+    double kkt[2], relp[2], reld[2], relg[2];
+    const bool have_avg = S.W > 0.0;
+    for (int c = 0; c < 2; ++c) {
+        const double pobj = cq[4 + c];
+        const double dobj = rq[4 + c] + cq[6 + c];
+        const double gap = fabs(pobj - dobj);
+        relp[c] = rq[2 + c] / (1.0 + S.b_inf);
+        reld[c] = cq[2 + c] / (1.0 + S.c_inf);
+        relg[c] = gap / (1.0 + fabs(pobj) + fabs(dobj));
+        kkt[c] = sqrt(S.omega * rq[0 + c] + cq[0 + c] / S.omega + gap * gap);
+        S.pobj[c] = pobj;
+        S.dobj[c] = dobj;
+        S.rel_p[c] = relp[c];
+        S.rel_d[c] = reld[c];
+        S.rel_g[c] = relg[c];
+    }
+    if (!have_avg) kkt[1] = INFINITY;
+    S.evals += 1;
+    S.avg_pending = 0;
+    S.restart_flag = 0;
+    if (!(kkt[0] == kkt[0])) {
+        S.done = 3;
+        S.out_sel = 0;
+        atomicAdd(done_count, 1u);
+        return;
+    }
+    // termination: current first, then the average
+    for (int c = 0; c < 2; ++c) {
+        if (c == 1 && !have_avg) break;
+        if (relp[c] <= S.tol_p && reld[c] <= S.tol_d && relg[c] <= S.tol_g) {
+            S.done = 1;
+            S.out_sel = c;
+            atomicAdd(done_count, 1u);
+            return;
+        }
+    }
+    const int cand = kkt[1] < kkt[0] ? 1 : 0;
+    if (S.attempts >= S.max_attempts) {
+        S.done = 2;
+        S.out_sel = cand;
+        atomicAdd(done_count, 1u);
+        return;
+    }
+    const double worst = fmax(relp[cand] / S.tol_p, fmax(reld[cand] / S.tol_d, relg[cand] / S.tol_g));
+    if (S.compensated == 2 || (S.compensated == 1 && worst < 100.0)) S.refine = 1;
+    const double kc = kkt[cand];
+    if (S.evals == 1) {  // initial point: record it as the last restart point
+        S.kkt_last = kc;
+        S.kkt_prev = kc;
+        S.restart_flag = 1;
+        return;
+    }
+    if (!S.enable_restart) return;
+    const bool restart = kc <= S.beta_suff * S.kkt_last ||
+                         (kc <= S.beta_nec * S.kkt_last && kc > S.kkt_prev) ||
+                         (double)S.since_restart >= S.beta_art * (double)S.steps;
+    S.kkt_prev = kc;
+    if (!restart) return;
+    const double dxn = sqrt(S.col_eval_dist[cand]), dyn = sqrt(S.row_eval[6 + cand]);
+    if (dxn > 1e-10 && dyn > 1e-10) {
+        const double th = S.weight_smoothing;
+        S.omega = exp(th * log(dyn / dxn) + (1.0 - th) * log(S.omega));
+    }
+    S.kkt_last = kc;
+    S.restart_flag = cand == 1 ? 2 : 1;
+    S.restarts += 1;
+    S.since_restart = 0;
+    S.W = 0.0;
+}
+
+// Column evaluation of both candidates: reduced cost lambda = c + K^T y_c,
+// dual residual (the parts no finite bound carries; scaled 2-norm^2 and
+// original inf-norm), primal objective, column part of the dual objective,
+// |x_c - x_last|^2.  The warp completing an instance runs its controller.
+struct EvalColsEpi {
+    Vecs V;
+    unsigned* done_count;
+    const float *yg[2], *xc;
+    Acc d2[2], pobj[2], dterm[2], dxl2[2];
+    float dinf[2];
+    struct Pre { float c, l, u, dc, xc, xa, xl; };
+    __device__ Pre pre(int j) const {
+        return Pre{V.c[j], V.l[j], V.u[j], V.dcol[j], xc[j], V.x_avg[j], V.x_last[j]};
+    }
+    __device__ void begin(const Inst& S) {
+        yg[0] = pick(V.y0, V.y1, S.cur);
+        yg[1] = V.y_avg;
+        xc = pick(V.x0, V.x1, S.cur);
+    }
+    __device__ const float* gather(int v) const { return yg[v]; }
+    __device__ void apply(int j, const SegDot<2>& d, const Pre& p) {
+        V.kty_eval[j] = d.f(1);
+        const float xv[2] = {p.xc, p.xa};
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            float h, lo;  // lambda = c + (s + e) as the float-float h + lo
+            two_sum(p.c, d.s[k], h, lo);
+            lo = __fadd_rn(lo, d.e[k]);
+            const float lam = __fadd_rn(h, lo);
+            float rd = 0.f;
+            if (lam > 0.f) {
+                if (fin(p.l)) { dterm[k].add_prod(h, p.l); dterm[k].add(lo * p.l); } else rd = lam;
+            } else if (lam < 0.f) {
+                if (fin(p.u)) { dterm[k].add_prod(h, p.u); dterm[k].add(lo * p.u); } else rd = -lam;
+            }
+            d2[k].add(rd * rd);
+            dinf[k] = fmaxf(dinf[k], rd / p.dc);
+            pobj[k].add_prod(p.c, xv[k]);
+            const float dx = xv[k] - p.xl;
+            dxl2[k].add(dx * dx);
+        }
+    }
+    __device__ void values(double (&q)[10]) {
+        const double v[10] = {d2[0].value(),   d2[1].value(),   (double)dinf[0], (double)dinf[1],
+                              pobj[0].value(), pobj[1].value(), dterm[0].value(), dterm[1].value(),
+                              dxl2[0].value(), dxl2[1].value()};
+        for (int k = 0; k < 10; ++k) q[k] = v[k];
+        for (int k = 0; k < 2; ++k) {
+            d2[k].reset();
+            pobj[k].reset();
+            dterm[k].reset();
+            dxl2[k].reset();
+            dinf[k] = 0.f;
+        }
+    }
+    __device__ void finish(Inst& S, const double* tot) {
+        S.col_eval_dist[0] = tot[8];
+        S.col_eval_dist[1] = tot[9];
+        eval_controller(S, tot, done_count);
+    }
+};
+
+__global__ void __launch_bounds__(kThreads) k_eval_cols(Side cols, Vecs V, Inst* __restrict__ st,
+                                                        unsigned* done_count) {
+    EvalColsEpi epi{V, done_count};
+    block_engine<2, true, 10>(cols, st, epi, 0x0Cu);
+}
+
+// Applies a restart decided by the evaluation: restart to the average copies
+// the average point (and its products from the evaluation) into the current
+// buffers; either restart makes the new current point the last restart point
+// and the start of the next average.
+__global__ void __launch_bounds__(kThreads) k_restart(Side cols, Side rows, Vecs V, Inst* __restrict__ st) {
+    for_each_segment_both(cols, rows, st, [&](bool is_col, const Inst& S, int r) {
+        const int flag = S.restart_flag;
+        if (flag == 0) return;
+        if (is_col) {
+            float* x = pick(V.x0, V.x1, S.cur);
+            if (flag == 2) {
+                x[r] = V.x_avg[r];
+                pick(V.kty0, V.kty1, S.cur)[r] = V.kty_eval[r];
+            }
+            V.x_last[r] = x[r];
+            V.x_acc[r] = make_float2(x[r], 0.f);
+        } else {
+            float* y = pick(V.y0, V.y1, S.cur);
+            if (flag == 2) {
+                y[r] = V.y_avg[r];
+                pick(V.kx0, V.kx1, S.cur)[r] = V.kx_eval[r];
+            }
+            V.y_last[r] = y[r];
+            V.y_acc[r] = make_float2(y[r], 0.f);
+        }
+    });
+}
+
+// ---------------------------------------------------------------- setup kernels
+// Per-segment max |a| (mode 0) or sum |a| (mode 1) -> scale 1/sqrt(.) (1 if 0).
+__global__ void k_seg_scale(SegMatrix A, int mode, float* __restrict__ scale) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < A.nseg; s += gridDim.x * blockDim.x) {
+        float acc = 0.f;
+        for (int k = A.ptr[s]; k < A.ptr[s + 1]; ++k) {
+            const float a = fabsf(__int_as_float(A.pairs[k].y));
+            acc = mode == 0 ? fmaxf(acc, a) : acc + a;
+        }
+        scale[s] = acc > 0.f ? 1.0f / sqrtf(acc) : 1.0f;
+    }
+}
+
+// a <- a * own[seg] * other[index] for every entry of one side.
+__global__ void k_scale_entries(SegMatrix A, const float* __restrict__ own, const float* __restrict__ other) {
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < A.nseg; s += gridDim.x * blockDim.x) {
+        const float fs = own[s];
+        for (int k = A.ptr[s]; k < A.ptr[s + 1]; ++k) {
+            int2 p = A.pairs[k];
+            p.y = __float_as_int(__int_as_float(p.y) * fs * other[p.x]);
+            const_cast<int2*>(A.pairs)[k] = p;
+        }
+    }
+}
+
+__global__ void k_mul_inplace(int n, float* __restrict__ acc, const float* __restrict__ f) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc[i] *= f[i];
+}
+
+// Scaled data: c~ = c d, l~ = l / d, u~ = u / d; rl~ = rl r, ru~ = ru r.
+__global__ void k_scale_vectors(int N, int M, float* c, float* l, float* u, const float* dcol, float* rl, float* ru,
+                                const float* drow) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
+        c[j] *= dcol[j];
+        l[j] /= dcol[j];
+        u[j] /= dcol[j];
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+        rl[i] *= drow[i];
+        ru[i] *= drow[i];
+    }
+}
+
+// Per-instance statistics of the scaled problem for the initial step size and
+// primal weight: rows give max |a~| and |b~|^2, columns give |c~|^2.
+template <bool ROWS>
+__device__ void init_stats_side(const Side& sd, const Vecs& V, Inst* st) {
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+    const int rb = sd.block_run_begin[blockIdx.x], re = sd.block_run_begin[blockIdx.x + 1];
+    for (int run = rb; run < re; ++run) {
+        const Run R = sd.runs[run];
+        float amax = 0.f;
+        Acc sq;
+        for (int ti = R.task_begin + warp; ti < R.task_end; ti += nwarps) {
+            const Task t = sd.tasks[ti];
+            if (t.flags & kTaskList) continue;  // light tasks cover every segment and nonzero
+            const int k0 = sd.A.ptr[t.seg_begin], k1 = sd.A.ptr[t.seg_end];
+            for (int k = k0 + lane; k < k1; k += 32) amax = fmaxf(amax, fabsf(__int_as_float(sd.A.pairs[k].y)));
+            for (int s = t.seg_begin + lane; s < t.seg_end; s += 32) {
+                if (ROWS) {
+                    const float lo = V.rl[s], hi = V.ru[s];
+                    const float b = fin(lo) ? lo : (fin(hi) ? hi : 0.f);
+                    sq.add_prod(b, b);
+                } else {
+                    sq.add_prod(V.c[s], V.c[s]);
+                }
+            }
+        }
+        const double q[2] = {(double)amax, sq.value()};
+        double tot[2];
+        if (run_reduce<2>(sd, run, R.inst, q, 0x1u, tot) && threadIdx.x == 0) {
+            Inst& S = st[R.inst];
+            if (ROWS) {
+                S.kmax = tot[0];
+                S.b2 = tot[1];
+            } else {
+                S.c2 = tot[1];
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_init_stats_rows(Side rows, Vecs V, Inst* __restrict__ st) {
+    init_stats_side<true>(rows, V, st);
+}
+__global__ void __launch_bounds__(kThreads) k_init_stats_cols(Side cols, Vecs V, Inst* __restrict__ st) {
+    init_stats_side<false>(cols, V, st);
+}
+
+__global__ void k_init_controller(int B, Inst* st, double step_scale) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    Inst& S = st[b];
+    S.eta = S.kmax > 0.0 ? step_scale / S.kmax : 1.0;
+    const double cn = sqrt(S.c2), bn = sqrt(S.b2);
+    S.omega = (cn > 1e-10 && bn > 1e-10) ? cn / bn : 1.0;
+}
+
+// Initial point x = clip(0, l~, u~) in both buffers, as the average and as the
+// last restart point; y = 0 everywhere; K^T y = 0.
+__global__ void k_init_point(int N, int M, Vecs V) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
+        const float x = fminf(fmaxf(0.0f, V.l[j]), V.u[j]);
+        V.x0[j] = x;
+        V.x1[j] = x;
+        V.x_avg[j] = x;
+        V.x_last[j] = x;
+        V.x_acc[j] = make_float2(x, 0.f);
+        V.kty0[j] = 0.f;
+        V.kty1[j] = 0.f;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) {
+        V.y0[i] = 0.f;
+        V.y1[i] = 0.f;
+        V.y_avg[i] = 0.f;
+        V.y_last[i] = 0.f;
+        V.y_acc[i] = make_float2(0.f, 0.f);
+    }
+}
+
+// y = K x for the initial point (row tasks, plain FP32 sums).
+struct StoreEpi {
+    const float* vec;
+    float* out;
+    struct Pre {};
+    __device__ Pre pre(int) const { return Pre{}; }
+    __device__ void begin(const Inst&) {}
+    __device__ const float* gather(int) const { return vec; }
+    __device__ void apply(int i, const SegDot<1>& d, const Pre&) { out[i] = d.s[0]; }
+    __device__ void values(double (&q)[1]) { q[0] = 0.0; }
+    __device__ void finish(Inst&, const double*) {}
+};
+
+__global__ void __launch_bounds__(kThreads) k_spmv_store(Side side, Inst* __restrict__ st, const float* __restrict__ vec,
+                                                         float* __restrict__ out) {
+    StoreEpi epi{vec, out};
+    block_engine<1, false, 1>(side, st, epi, 0u);
+}
+
+// ---------------------------------------------------------------- host: schedule
+static int pow2_floor(int v) {
+    int p = 1;
+    while (p * 2 <= v) p *= 2;
+    return p;
+}
+
+void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, int blocks,
+                   SideSchedule& out) {
+    const int B = (int)inst_off.size() - 1;
+    out = SideSchedule{};
+    out.light_max.assign(B, 0);
+    for (int b = 0; b < B; ++b) {
+        const int s0 = inst_off[b], s1 = inst_off[b + 1];
+        const long long nnz = ptr[s1] - ptr[s0];
+        const int nseg = s1 - s0;
+        const int mean = nseg > 0 ? (int)((nnz + nseg - 1) / nseg) : 1;
+        // light segments: up to two load batches per lane of the instance's mean lane group
+        const int L0 = std::max(1, std::min(32, pow2_floor(std::max(1, mean / kBatch))));
+        const int lmax = std::max(2 * kBatch * L0, 8);
+        out.light_max[b] = lmax;
+        // light tasks: contiguous, at most task_nnz light nonzeros / kTaskSegs segments
+        int s = s0;
+        while (s < s1) {
+            int e = s;
+            long long acc = 0;
+            while (e < s1 && e - s < kTaskSegs) {
+                const int len = ptr[e + 1] - ptr[e];
+                const long long add = len > lmax ? 0 : len;
+                if (e > s && acc + add > task_nnz) break;
+                acc += add;
+                ++e;
+            }
+            const int nl = std::max(1, e - s);
+            const int L = std::max(1, std::min(32, pow2_floor(std::max(1, (int)(acc / nl) / kBatch))));
+            out.tasks.push_back(Task{s, e, b, L << 8});
+            s = e;
+        }
+        // list tasks: longer segments by length class (2 lmax, 4 lmax, ...], lanes doubling per class
+        for (int cls = 1, lo = lmax, L = std::min(32, 2 * L0); lo < (1 << 30); ++cls, lo *= 2, L = std::min(32, 2 * L)) {
+            const int hi = (L == 32) ? (1 << 30) : 2 * lo;
+            const int hb = (int)out.list_idx.size();
+            for (int r = s0; r < s1; ++r) {
+                const int len = ptr[r + 1] - ptr[r];
+                if (len > lo && len <= hi) out.list_idx.push_back(r);
+            }
+            int h = hb;
+            while (h < (int)out.list_idx.size()) {
+                int e = h;
+                long long acc = 0;
+                while (e < (int)out.list_idx.size()) {
+                    const int len = ptr[out.list_idx[e] + 1] - ptr[out.list_idx[e]];
+                    if (e > h && acc + len > task_nnz) break;
+                    acc += len;
+                    ++e;
+                }
+                out.tasks.push_back(Task{h, e, b, kTaskList | (L << 8)});
+                h = e;
+            }
+            if (L == 32) break;
+        }
+    }
+    // contiguous, work-balanced task ranges per block, cut into per-instance runs
+    const int nt = (int)out.tasks.size();
+    std::vector<double> pre(nt + 1, 0.0);
+    for (int t = 0; t < nt; ++t) {
+        const Task& k = out.tasks[t];
+        double w = 64.0;
+        if (k.flags & kTaskList) {
+            for (int h = k.seg_begin; h < k.seg_end; ++h)
+                w += 16.0 + (ptr[out.list_idx[h] + 1] - ptr[out.list_idx[h]]);
+        } else {
+            w += (ptr[k.seg_end] - ptr[k.seg_begin]) + 8.0 * (k.seg_end - k.seg_begin);
+        }
+        pre[t + 1] = pre[t] + w;
+    }
+    blocks = std::max(1, blocks);
+    out.block_run_begin.assign(blocks + 1, 0);
+    int t = 0;
+    for (int g = 0; g < blocks; ++g) {
+        out.block_run_begin[g] = (int)out.runs.size();
+        int te = t;
+        const double target = pre[nt] * (g + 1) / blocks;
+        while (te < nt && (g == blocks - 1 || pre[te + 1] <= target)) ++te;
+        while (t < te) {
+            int e = t;
+            while (e < te && out.tasks[e].inst == out.tasks[t].inst) ++e;
+            out.runs.push_back(Run{out.tasks[t].inst, t, e, 0});
+            t = e;
+        }
+    }
+    out.block_run_begin[blocks] = (int)out.runs.size();
+    out.inst_run_begin.assign(B + 1, (int)out.runs.size());
+    for (int r = (int)out.runs.size() - 1; r >= 0; --r) out.inst_run_begin[out.runs[r].inst] = r;
+    for (int b = B - 1; b >= 0; --b) out.inst_run_begin[b] = std::min(out.inst_run_begin[b], out.inst_run_begin[b + 1]);
+}
+
+// ---------------------------------------------------------------- host: solver
+MixedSolver::~MixedSolver() {
+    for (auto& g : graphs_)
+        if (g) cudaGraphExecDestroy(g);
+    if (ev_start_) cudaEventDestroy(ev_start_);
+    if (ev_stop_) cudaEventDestroy(ev_stop_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+static int upload(DevMem& d, const void* h, size_t bytes, cudaStream_t s) {
+    SIHG_TRY(d.alloc(bytes));
+    if (bytes) SIHG_CUDA(cudaMemcpyAsync(d.as<void>(), h, bytes, cudaMemcpyHostToDevice, s));
+    return SIH_PDHG_OK;
+}
+
+int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_pdhg_config& cfg,
+                       const sih_pdhg_options& opts) {
+    probs_ = probs;
+    cfg_ = cfg;
+    opts_ = opts;
+    B_ = (int)probs.size();
+    int dev = 0;
+    SIHG_CUDA(cudaGetDevice(&dev));
+    SIHG_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, dev));
+    SIHG_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    SIHG_CUDA(cudaEventCreate(&ev_start_));
+    SIHG_CUDA(cudaEventCreate(&ev_stop_));
+    cudaStream_t s = stream_;
+
+    // ---- concatenate the instances (block-diagonal), global indices
+    row_off_.assign(B_ + 1, 0);
+    col_off_.assign(B_ + 1, 0);
+    long long nnz = 0;
+    for (int b = 0; b < B_; ++b) {
+        row_off_[b + 1] = row_off_[b] + probs[b]->m;
+        col_off_[b + 1] = col_off_[b] + probs[b]->n;
+        nnz += probs[b]->nnz;
+    }
+    M_ = row_off_[B_];
+    N_ = col_off_[B_];
+    nnz_ = nnz;
+    if ((long long)M_ >= INT32_MAX - 64 || (long long)N_ >= INT32_MAX - 64 || nnz >= INT32_MAX - 64)
+        return fail(SIH_PDHG_ERR_UNSUPPORTED, "batch exceeds the 32-bit index layout");
+    std::vector<int> csr_ptr((size_t)M_ + 1), csc_ptr((size_t)N_ + 1);
+    std::vector<Pair> csr((size_t)nnz), csc((size_t)nnz);
+    std::vector<float> c(N_), l(N_), u(N_), rl(M_), ru(M_);
+    {
+        std::vector<long long> k_off(B_ + 1, 0);
+        for (int b = 0; b < B_; ++b) k_off[b + 1] = k_off[b] + probs[b]->nnz;
+        parallel_for(B_, [&](int64_t b0, int64_t b1) {
+            for (int64_t b = b0; b < b1; ++b) {
+                const HostProblem& p = *probs[b];
+                const int ro = row_off_[b], co = col_off_[b];
+                const long long ko = k_off[b];
+                for (int i = 0; i < p.m; ++i) csr_ptr[ro + i] = (int)(p.csr_ptr[i] + ko);
+                for (int j = 0; j < p.n; ++j) csc_ptr[co + j] = (int)(p.csc_ptr[j] + ko);
+                for (int k = 0; k < p.nnz; ++k) {
+                    csr[ko + k] = Pair{p.csr[k].idx + co, p.csr[k].val};
+                    csc[ko + k] = Pair{p.csc[k].idx + ro, p.csc[k].val};
+                }
+                // infinite bounds are +-inf (|v| >= 1e20 counts as infinite)
+                auto inf_clean = [](double v) -> float {
+                    if (std::isinf(v) || std::fabs(v) >= 1e20) return v > 0 ? INFINITY : -INFINITY;
+                    return (float)v;
+                };
+                for (int j = 0; j < p.n; ++j) {
+                    c[co + j] = p.c[j];
+                    l[co + j] = inf_clean(p.src->col_lower[j]);
+                    u[co + j] = inf_clean(p.src->col_upper[j]);
+                }
+                for (int i = 0; i < p.m; ++i) {
+                    rl[ro + i] = inf_clean(p.src->row_lower[i]);
+                    ru[ro + i] = inf_clean(p.src->row_upper[i]);
+                }
+            }
+        });
+        csr_ptr[M_] = (int)nnz;
+        csc_ptr[N_] = (int)nnz;
+    }
+    // ---- schedules (tasks, block ranges, runs)
+    int occ = 0;
+    SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_step_dual, kThreads, 0));
+    grid_ = std::max(1, sm_count_ * std::max(1, occ));
+    // default task size: about four tasks per resident warp, within [128, 2048]
+    const long long warps = (long long)grid_ * (kThreads / 32);
+    task_nnz_ = opts.tile_nnz > 0 ? opts.tile_nnz
+                                  : (int)std::max(128LL, std::min(2048LL, nnz / std::max(1LL, 4 * warps)));
+    task_nnz_ = std::max(32, std::min(1 << 20, task_nnz_));
+    SideSchedule rs, cs;
+    make_schedule(csr_ptr, row_off_, task_nnz_, grid_, rs);
+    make_schedule(csc_ptr, col_off_, task_nnz_, grid_, cs);
+
+    SIHG_TRY(upload(csr_ptr_, csr_ptr.data(), sizeof(int) * csr_ptr.size(), s));
+    SIHG_TRY(upload(csc_ptr_, csc_ptr.data(), sizeof(int) * csc_ptr.size(), s));
+    SIHG_TRY(upload(csr_pairs_, csr.data(), sizeof(Pair) * csr.size(), s));
+    SIHG_TRY(upload(csc_pairs_, csc.data(), sizeof(Pair) * csc.size(), s));
+    auto upload_schedule = [&](const SideSchedule& sc, DevMem& mem, const SegMatrix& A, DevMem& part,
+                               unsigned* tickets, Side& side) -> int {
+        const size_t nt = sc.tasks.size(), nr = sc.runs.size();
+        const size_t bytes = sizeof(Task) * nt + sizeof(Run) * nr +
+                             sizeof(int) * (sc.block_run_begin.size() + sc.inst_run_begin.size() +
+                                            sc.list_idx.size() + sc.light_max.size()) + 64;
+        std::vector<char> buf(bytes, 0);
+        size_t off = 0;
+        auto put = [&](const void* src, size_t n) {
+            const size_t at = off;
+            if (n) std::memcpy(buf.data() + off, src, n);
+            off += (n + 15) & ~(size_t)15;
+            return at;
+        };
+        const size_t o_t = put(sc.tasks.data(), sizeof(Task) * nt);
+        const size_t o_r = put(sc.runs.data(), sizeof(Run) * nr);
+        const size_t o_b = put(sc.block_run_begin.data(), sizeof(int) * sc.block_run_begin.size());
+        const size_t o_i = put(sc.inst_run_begin.data(), sizeof(int) * sc.inst_run_begin.size());
+        const size_t o_h = put(sc.list_idx.data(), sizeof(int) * sc.list_idx.size());
+        const size_t o_x = put(sc.light_max.data(), sizeof(int) * sc.light_max.size());
+        buf.resize(std::max<size_t>(off, 16));
+        SIHG_TRY(upload(mem, buf.data(), buf.size(), s));
+        SIHG_TRY(part.alloc(sizeof(double) * kQ * std::max<size_t>(1, nr)));
+        char* d = mem.as<char>();
+        side = Side{A, (const Task*)(d + o_t), (int)nt, (const Run*)(d + o_r), (const int*)(d + o_b),
+                    (const int*)(d + o_i), (const int*)(d + o_h), (const int*)(d + o_x), part.as<double>(), tickets};
+        return SIH_PDHG_OK;
+    };
+    SIHG_TRY(tickets_.alloc(sizeof(unsigned) * 2 * (B_ + 1)));
+    SIHG_CUDA(cudaMemsetAsync(tickets_.as<void>(), 0, sizeof(unsigned) * 2 * (B_ + 1), s));
+    SIHG_TRY(upload_schedule(rs, row_sched_, SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()}, row_part_,
+                             tickets_.as<unsigned>(), rows_));
+    SIHG_TRY(upload_schedule(cs, col_sched_, SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, col_part_,
+                             tickets_.as<unsigned>() + (B_ + 1), cols_));
+
+    // ---- vectors: 11 column vectors, 10 row vectors (layout of Vecs) + float-float averages
+    SIHG_TRY(colvec_.alloc(sizeof(float) * (size_t)N_ * 11));
+    SIHG_TRY(rowvec_.alloc(sizeof(float) * (size_t)M_ * 10));
+    SIHG_TRY(accvec_.alloc(sizeof(float2) * ((size_t)N_ + M_)));
+    float* cv = colvec_.as<float>();
+    float* rv = rowvec_.as<float>();
+    auto C = [&](int k) { return cv + (size_t)k * N_; };
+    auto R = [&](int k) { return rv + (size_t)k * M_; };
+    V_ = Vecs{C(0), C(1), C(2), C(3), C(4), C(5), C(6), C(7), C(8), C(9), C(10),
+              R(0), R(1), R(2), R(3), R(4), R(5), R(6), R(7), R(8), R(9),
+              accvec_.as<float2>(), accvec_.as<float2>() + N_};
+    SIHG_CUDA(cudaMemcpyAsync(C(0), c.data(), sizeof(float) * N_, cudaMemcpyHostToDevice, s));
+    SIHG_CUDA(cudaMemcpyAsync(C(1), l.data(), sizeof(float) * N_, cudaMemcpyHostToDevice, s));
+    SIHG_CUDA(cudaMemcpyAsync(C(2), u.data(), sizeof(float) * N_, cudaMemcpyHostToDevice, s));
+    SIHG_CUDA(cudaMemcpyAsync(R(0), rl.data(), sizeof(float) * M_, cudaMemcpyHostToDevice, s));
+    SIHG_CUDA(cudaMemcpyAsync(R(1), ru.data(), sizeof(float) * M_, cudaMemcpyHostToDevice, s));
+
+    // ---- scaling (Ruiz inf-norm passes, then Pock-Chambolle alpha = 1)
+    std::vector<float> ones_c(N_, 1.0f), ones_r(M_, 1.0f);
+    SIHG_CUDA(cudaMemcpyAsync(C(3), ones_c.data(), sizeof(float) * N_, cudaMemcpyHostToDevice, s));
+    SIHG_CUDA(cudaMemcpyAsync(R(2), ones_r.data(), sizeof(float) * M_, cudaMemcpyHostToDevice, s));
+    DevMem tmp;
+    SIHG_TRY(tmp.alloc(sizeof(float) * ((size_t)N_ + M_ + 8)));
+    float* fc = tmp.as<float>();
+    float* fr = fc + N_;
+    const int g = sm_count_ * 8;
+    auto scale_pass = [&](int mode) -> int {
+        k_seg_scale<<<g, 256, 0, s>>>(cols_.A, mode, fc);
+        k_seg_scale<<<g, 256, 0, s>>>(rows_.A, mode, fr);
+        k_scale_entries<<<g, 256, 0, s>>>(rows_.A, fr, fc);
+        k_scale_entries<<<g, 256, 0, s>>>(cols_.A, fc, fr);
+        k_mul_inplace<<<g, 256, 0, s>>>(N_, C(3), fc);
+        k_mul_inplace<<<g, 256, 0, s>>>(M_, R(2), fr);
+        SIHG_LAUNCH_CHECK();
+        return SIH_PDHG_OK;
+    };
+    for (int k = 0; k < opts.ruiz_iterations; ++k) SIHG_TRY(scale_pass(0));
+    if (opts.pock_chambolle) SIHG_TRY(scale_pass(1));
+    k_scale_vectors<<<g, 256, 0, s>>>(N_, M_, C(0), C(1), C(2), C(3), R(0), R(1), R(2));
+    SIHG_LAUNCH_CHECK();
+    SIHG_CUDA(cudaStreamSynchronize(s));  // tmp is released at scope end
+
+    // ---- per-instance state
+    SIHG_TRY(state_.alloc(sizeof(Inst) * B_));
+    SIHG_TRY(done_count_.alloc(sizeof(unsigned)));
+    host_inst_.assign(B_, Inst{});
+    for (int b = 0; b < B_; ++b) {
+        Inst& S = host_inst_[b];
+        std::memset(&S, 0, sizeof(Inst));
+        const sih_pdhg_problem* p = probs[b]->src;
+        double binf = 0.0, cinf = 0.0;
+        for (int64_t i = 0; i < p->num_rows; ++i) {
+            if (bound_is_finite(p->row_lower[i])) binf = std::max(binf, std::fabs(p->row_lower[i]));
+            if (bound_is_finite(p->row_upper[i])) binf = std::max(binf, std::fabs(p->row_upper[i]));
+        }
+        for (int64_t j = 0; j < p->num_cols; ++j) cinf = std::max(cinf, std::fabs(p->c[j]));
+        S.b_inf = binf;
+        S.c_inf = cinf;
+        S.tol_p = cfg.tol_primal;
+        S.tol_d = cfg.tol_dual;
+        S.tol_g = cfg.tol_gap;
+        S.max_attempts = cfg.max_iterations;
+        S.enable_restart = cfg.enable_restart ? 1 : 0;
+        S.compensated = opts.compensated;
+        S.refine = opts.compensated == 2 ? 1 : 0;
+        S.beta_suff = opts.restart_sufficient;
+        S.beta_nec = opts.restart_necessary;
+        S.beta_art = opts.restart_artificial;
+        S.weight_smoothing = opts.primal_weight_smoothing;
+    }
+    return SIH_PDHG_OK;
+}
+
+int MixedSolver::launch_step(cudaStream_t s) {
+    Inst* st = state_.as<Inst>();
+    k_step_primal<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
+    k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
+    k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
+    SIHG_LAUNCH_CHECK();
+    return SIH_PDHG_OK;
+}
+
+int MixedSolver::launch_eval(cudaStream_t s) {
+    Inst* st = state_.as<Inst>();
+    k_flush_avg<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
+    k_eval_rows<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
+    k_eval_cols<<<grid_, kThreads, 0, s>>>(cols_, V_, st, done_count_.as<unsigned>());
+    k_restart<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
+    SIHG_LAUNCH_CHECK();
+    return SIH_PDHG_OK;
+}
+
+int MixedSolver::reset_state() {
+    cudaStream_t s = stream_;
+    const int g = sm_count_ * 4;
+    for (int b = 0; b < B_; ++b) {
+        Inst& S = host_inst_[b];
+        S.done = 0;
+        S.cur = 0;
+        S.avg_pending = 0;
+        S.restart_flag = 0;
+        S.refine = opts_.compensated == 2 ? 1 : 0;
+        S.out_sel = 0;
+        S.attempts = S.steps = S.rejections = S.restarts = S.since_restart = S.evals = 0;
+        S.W = 0.0;
+        S.avg_w = 0.0;
+        S.kkt_last = S.kkt_prev = 0.0;
+    }
+    SIHG_CUDA(cudaMemcpyAsync(state_.as<Inst>(), host_inst_.data(), sizeof(Inst) * B_, cudaMemcpyHostToDevice, s));
+    SIHG_CUDA(cudaMemsetAsync(done_count_.as<void>(), 0, sizeof(unsigned), s));
+    // initial point x = clip(0, l~, u~), y = 0; averages and last points equal it
+    k_init_point<<<g, 256, 0, s>>>(N_, M_, V_);
+    SIHG_LAUNCH_CHECK();
+    k_spmv_store<<<grid_, kThreads, 0, s>>>(rows_, state_.as<Inst>(), V_.x0, V_.kx0);
+    k_init_stats_rows<<<grid_, kThreads, 0, s>>>(rows_, V_, state_.as<Inst>());
+    k_init_stats_cols<<<grid_, kThreads, 0, s>>>(cols_, V_, state_.as<Inst>());
+    k_init_controller<<<(B_ + 127) / 128, 128, 0, s>>>(B_, state_.as<Inst>(), 1.0);
+    SIHG_LAUNCH_CHECK();
+    // initial evaluation: KKT of the starting point (no restart decision)
+    SIHG_TRY(launch_eval(s));
+    return SIH_PDHG_OK;
+}
+
+int MixedSolver::record_graph() {
+    if (graphs_[0]) return SIH_PDHG_OK;
+    cudaGraph_t g = nullptr;
+    SIHG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    int rc = SIH_PDHG_OK;
+    for (int k = 0; k < eval_freq_ && rc == SIH_PDHG_OK; ++k) rc = launch_step(stream_);
+    if (rc == SIH_PDHG_OK) rc = launch_eval(stream_);
+    cudaError_t e = cudaStreamEndCapture(stream_, &g);
+    if (rc != SIH_PDHG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    e = cudaGraphInstantiate(&graphs_[0], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    return SIH_PDHG_OK;
+}
+
+int MixedSolver::run() {
+    eval_freq_ = opts_.eval_frequency > 0 ? opts_.eval_frequency : 64;
+    if (opts_.use_graph) SIHG_TRY(record_graph());
+    const auto t0 = std::chrono::steady_clock::now();
+    SIHG_TRY(reset_state());
+    cudaStream_t s = stream_;
+    constexpr int kWindow = 3;
+    unsigned* h_done = nullptr;
+    SIHG_CUDA(cudaHostAlloc(&h_done, sizeof(unsigned) * kWindow, cudaHostAllocDefault));
+    cudaEvent_t ev[kWindow] = {};
+    int rc = SIH_PDHG_OK;
+    for (int w = 0; w < kWindow && rc == SIH_PDHG_OK; ++w) {
+        h_done[w] = 0;
+        cudaError_t e = cudaEventCreateWithFlags(&ev[w], cudaEventDisableTiming);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate", __FILE__, __LINE__);
+    }
+    const long long max_blocks = (cfg_.max_iterations + eval_freq_ - 1) / eval_freq_ + 1;
+    timed_out_ = false;
+    if (rc == SIH_PDHG_OK) {
+        cudaEventRecord(ev_start_, s);
+        for (long long blk = 0; blk < max_blocks && rc == SIH_PDHG_OK; ++blk) {
+            const int slot = (int)(blk % kWindow);
+            if (blk >= kWindow) {
+                cudaError_t e = cudaEventSynchronize(ev[slot]);
+                if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__); break; }
+                if ((int)h_done[slot] >= B_) break;
+                if (opts_.time_limit_sec > 0 &&
+                    std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > opts_.time_limit_sec) {
+                    timed_out_ = true;
+                    break;
+                }
+            }
+            if (opts_.use_graph) {
+                cudaError_t e = cudaGraphLaunch(graphs_[0], s);
+                if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
+            } else {
+                for (int k = 0; k < eval_freq_ && rc == SIH_PDHG_OK; ++k) rc = launch_step(s);
+                if (rc == SIH_PDHG_OK) rc = launch_eval(s);
+            }
+            cudaMemcpyAsync(&h_done[slot], done_count_.as<unsigned>(), sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+            cudaEventRecord(ev[slot], s);
+        }
+        cudaEventRecord(ev_stop_, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (rc == SIH_PDHG_OK && e != cudaSuccess) rc = cuda_fail(e, "iteration loop", __FILE__, __LINE__);
+    }
+    for (int w = 0; w < kWindow; ++w)
+        if (ev[w]) cudaEventDestroy(ev[w]);
+    cudaFreeHost(h_done);
+    if (rc != SIH_PDHG_OK) return rc;
+    SIHG_CUDA(cudaMemcpy(host_inst_.data(), state_.as<Inst>(), sizeof(Inst) * B_, cudaMemcpyDeviceToHost));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev_start_, ev_stop_);
+    loop_seconds_ = ms * 1e-3;
+    return SIH_PDHG_OK;
+}
+
+int MixedSolver::fetch(int b, std::vector<double>& x, std::vector<double>& y) {
+    const Inst& S = host_inst_[b];
+    const int n = probs_[b]->n, m = probs_[b]->m, co = col_off_[b], ro = row_off_[b];
+    std::vector<float> xs(n), ys(m), dc(n), dr(m);
+    const float* xsrc = S.out_sel == 1 ? V_.x_avg : (S.cur ? V_.x1 : V_.x0);
+    const float* ysrc = S.out_sel == 1 ? V_.y_avg : (S.cur ? V_.y1 : V_.y0);
+    SIHG_CUDA(cudaMemcpy(xs.data(), xsrc + co, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    SIHG_CUDA(cudaMemcpy(ys.data(), ysrc + ro, sizeof(float) * m, cudaMemcpyDeviceToHost));
+    SIHG_CUDA(cudaMemcpy(dc.data(), V_.dcol + co, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    SIHG_CUDA(cudaMemcpy(dr.data(), V_.drow + ro, sizeof(float) * m, cudaMemcpyDeviceToHost));
+    x.resize(n);
+    y.resize(m);
+    for (int j = 0; j < n; ++j) x[j] = (double)xs[j] * (double)dc[j];
+    for (int i = 0; i < m; ++i) y[i] = (double)ys[i] * (double)dr[i];
+    return SIH_PDHG_OK;
+}
+
+int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
+                sih_pdhg_result* r) {
+    MixedSolver solver;
+    std::vector<const HostProblem*> probs{&hp};
+    SIHG_TRY(solver.setup(probs, cfg, opts));
+    SIHG_TRY(solver.run());
+    std::vector<double> x, y;
+    SIHG_TRY(solver.fetch(0, x, y));
+    solver.fill_result(0, r);
+    pack_solution(hp.src, opts, x, y, r);
+    return SIH_PDHG_OK;
+}
+
+void MixedSolver::fill_result(int b, sih_pdhg_result* r) const {
+    const Inst& S = host_inst_[b];
+    switch (S.done) {
+        case 1: r->status = SIH_STATUS_OPTIMAL; break;
+        case 2: r->status = SIH_STATUS_ITERATION_LIMIT; break;
+        case 3: r->status = SIH_STATUS_NUMERICAL_FAILURE; break;
+        default: r->status = timed_out_ ? SIH_STATUS_TIME_LIMIT : SIH_STATUS_ITERATION_LIMIT; break;
+    }
+    r->iterations = S.attempts;
+    r->restarts = S.restarts;
+    r->step_rejections = S.rejections;
+    r->final_step = S.eta;
+    r->final_primal_weight = S.omega;
+    r->ref_primal = S.rel_p[S.out_sel];
+    r->ref_dual = S.rel_d[S.out_sel];
+    r->time_solver_sec = loop_seconds_;
+}
+
 }  // namespace sihg

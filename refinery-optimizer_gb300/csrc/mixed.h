@@ -1,10 +1,155 @@
-// Mixed-precision restarted adaptive PDHG (scaled, FP32 SpMV, FP64 reductions).
+// Mixed-precision restarted adaptive PDHG (scaled, FP32 SpMV, FP64 reductions)
+// for one LP or a batch of LPs; see mixed.cu for the algorithm.
 #pragma once
+
+#include <vector>
 
 #include "common.cuh"
 #include "host.h"
+#include "spmv.cuh"
 
 namespace sihg {
+
+constexpr int kQ = 12;         // partial slots per task
+constexpr int kThreads = 256;  // threads per block of every task kernel
+
+// Unit of SpMV work of one instance (see warp.cuh): a LIGHT task is the
+// contiguous segment range [seg_begin, seg_end) (longer segments skipped); a
+// LIST task holds list_idx[seg_begin..seg_end), segments of one length class.
+// `flags` bit 0 marks a list task, bits 8..15 hold the lanes per segment.
+struct Task {
+    int seg_begin;
+    int seg_end;
+    int inst;
+    int flags;
+};
+constexpr int kTaskList = 1;
+__host__ __device__ inline int task_lanes(int flags) { return (flags >> 8) & 0xff; }
+constexpr int kTaskSegs = 1024;  // max segments per light task
+
+// The tasks of one instance inside one block's task range.
+struct Run {
+    int inst;
+    int task_begin;
+    int task_end;
+    int pad;
+};
+
+// Per-instance device state (all reductions and controller scalars in FP64).
+struct Inst {
+    // control
+    int done;          // 0 running, 1 converged, 2 iteration limit, 3 numerical failure
+    int cur;           // buffer holding the current iterate (0 / 1)
+    int avg_pending;   // the averages still need the last accepted iterate (weight avg_w)
+    int restart_flag;  // set by an evaluation: 0 none, 1 restart at current, 2 restart at average
+    int refine;        // compensated (Dot2) evaluation SpMVs
+    int out_sel;       // returned point: 0 current, 1 average
+    int enable_restart;
+    int compensated;   // option: 0 off, 1 near tolerance, 2 always
+    long long attempts, steps, rejections, restarts, since_restart, evals, max_attempts;
+    // step size and primal weight
+    double eta, omega, W, avg_w;
+    double kkt_last, kkt_prev;
+    // reductions of the current attempt / evaluation
+    double dy2;
+    double row_eval[8];      // p2[2], pinf[2], dterm[2], dyl2[2]
+    double col_eval_dist[2]; // |x_c - x_last|^2
+    // last evaluation (index 0 current, 1 average)
+    double pobj[2], dobj[2], rel_p[2], rel_d[2], rel_g[2];
+    // constants
+    double b_inf, c_inf, tol_p, tol_d, tol_g;
+    double beta_suff, beta_nec, beta_art, weight_smoothing;
+    double kmax, b2, c2;
+};
+
+struct Side {
+    SegMatrix A;
+    const Task* tasks;
+    int ntasks;
+    const Run* runs;
+    const int* block_run_begin;  // [grid + 1]
+    const int* inst_run_begin;   // [B + 1]
+    const int* list_idx;         // segment ids of the list tasks
+    const int* light_max;        // [B] longest segment a light task processes
+    double* partials;            // [nruns * kQ]
+    unsigned* tickets;           // [B]
+};
+
+// Host-side schedule of one side.
+struct SideSchedule {
+    std::vector<Task> tasks;
+    std::vector<Run> runs;
+    std::vector<int> block_run_begin, inst_run_begin, list_idx, light_max;
+};
+
+// Host: tasks of every instance of one side (light tasks of at most task_nnz
+// light nonzeros, then list tasks per length class), cut into `blocks`
+// contiguous work-balanced ranges and per-instance runs.
+void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, int blocks,
+                   SideSchedule& out);
+
+struct Vecs {
+    // column side (length N)
+    const float *c, *l, *u, *dcol;
+    float *x0, *x1, *kty0, *kty1, *x_avg, *x_last, *kty_eval;
+    // row side (length M)
+    const float *rl, *ru, *drow;
+    float *y0, *y1, *kx0, *kx1, *y_avg, *y_last, *kx_eval;
+    // step-weighted running averages, accumulated in float-float (hi, lo);
+    // x_avg / y_avg above are their FP32 copies, refreshed before every evaluation
+    float2 *x_acc, *y_acc;
+};
+
+class MixedSolver {
+  public:
+    MixedSolver() = default;
+    MixedSolver(const MixedSolver&) = delete;
+    MixedSolver& operator=(const MixedSolver&) = delete;
+    ~MixedSolver();
+
+    // Concatenates the instances, uploads them, scales them on the device.
+    int setup(const std::vector<const HostProblem*>& probs, const sih_pdhg_config& cfg, const sih_pdhg_options& opts);
+    // Solves every instance from its initial point until all stop.
+    int run();
+    // Unscaled primal/dual point returned for instance b (PDHG sign).
+    int fetch(int b, std::vector<double>& x, std::vector<double>& y);
+    void fill_result(int b, sih_pdhg_result* r) const;
+
+    int instances() const { return B_; }
+    double loop_seconds() const { return loop_seconds_; }
+    cudaStream_t stream() const { return stream_; }
+    const Inst& inst(int b) const { return host_inst_[b]; }
+    int launch_step(cudaStream_t s);
+    int launch_eval(cudaStream_t s);
+    long long nnz() const { return nnz_; }
+    int rows() const { return M_; }
+    int cols() const { return N_; }
+
+  private:
+    int reset_state();
+    int record_graph();
+
+    std::vector<const HostProblem*> probs_;
+    sih_pdhg_config cfg_{};
+    sih_pdhg_options opts_{};
+    int B_ = 0, M_ = 0, N_ = 0;
+    long long nnz_ = 0;
+    int sm_count_ = 1;
+    int task_nnz_ = 1024;
+    int eval_freq_ = 64;
+    int grid_ = 1;
+    bool timed_out_ = false;
+    double loop_seconds_ = 0.0;
+    cudaStream_t stream_ = nullptr;
+    cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;
+    cudaGraphExec_t graphs_[1] = {nullptr};
+    std::vector<int> row_off_, col_off_;
+    DevMem csr_ptr_, csc_ptr_, csr_pairs_, csc_pairs_, row_sched_, col_sched_;
+    DevMem row_part_, col_part_, tickets_, colvec_, rowvec_, state_, done_count_, accvec_;
+    Side rows_{}, cols_{};
+    Vecs V_{};
+    std::vector<Inst> host_inst_;
+};
 
 int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
                 sih_pdhg_result* r);

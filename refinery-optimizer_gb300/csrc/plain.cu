@@ -26,79 +26,99 @@
 namespace sihg {
 
 // ---------------------------------------------------------------- kernels
+// Primal update of column j with z = (A^T y)_j (cuda_pdhg.cu:54-77).
+struct PrimalEpi {
+    PlainVecs v;
+    struct Pre { float x, c, tau, l, u; };
+    __device__ __forceinline__ Pre pre(int j) const { return Pre{v.x[j], v.c[j], v.tau[j], v.l[j], v.u[j]}; }
+    __device__ __forceinline__ void apply(int j, float aty, const Pre& p) const {
+        const float grad = __fadd_rn(p.c, aty);
+        float x_new = __fsub_rn(p.x, __fmul_rn(p.tau, grad));
+        if (x_new < p.l) x_new = p.l;
+        if (x_new > p.u) x_new = p.u;
+        v.x[j] = x_new;
+        v.xbar[j] = __fsub_rn(__fmul_rn(2.0f, x_new), p.x);
+    }
+};
+
+// Dual update of row i with w = (A x_bar)_i (cuda_pdhg.cu:82-103).
+struct DualEpi {
+    PlainVecs v;
+    struct Pre { float sig, y, rl, ru; };
+    __device__ __forceinline__ Pre pre(int i) const { return Pre{v.sigma[i], v.y[i], v.rl[i], v.ru[i]}; }
+    __device__ __forceinline__ void apply(int i, float axbar, const Pre& p) const {
+        const float w = __fadd_rn(axbar, p.y / p.sig);
+        float q = w;
+        if (q < p.rl) q = p.rl;
+        if (q > p.ru) q = p.ru;
+        v.y[i] = __fmul_rn(p.sig, __fsub_rn(w, q));
+    }
+};
+
+// Row violation of A x (cuda_pdhg.cu:114-129), running max per thread.
+struct RowViolEpi {
+    PlainVecs v;
+    float lmax;
+    struct Pre { float rl, ru; };
+    __device__ __forceinline__ Pre pre(int i) const { return Pre{v.rl[i], v.ru[i]}; }
+    __device__ __forceinline__ void apply(int, float ax, const Pre& p) {
+        float viol = 0.0f;
+        if (p.rl > -1e15f && ax < p.rl) viol = fmaxf(viol, __fsub_rn(p.rl, ax));
+        if (p.ru < 1e15f && ax > p.ru) viol = fmaxf(viol, __fsub_rn(ax, p.ru));
+        lmax = fmaxf(lmax, viol);
+    }
+};
+
+// Column measure |x - clip(x - tau (c + A^T y))| / max(1e-4, tau) (cuda_pdhg.cu:131-151).
+// fmaxf drops NaN measures, as the reference's host std::max does.
+struct ColMeasEpi {
+    PlainVecs v;
+    float lmax;
+    struct Pre { float x, c, tau, l, u; };
+    __device__ __forceinline__ Pre pre(int j) const { return Pre{v.x[j], v.c[j], v.tau[j], v.l[j], v.u[j]}; }
+    __device__ __forceinline__ void apply(int, float aty, const Pre& p) {
+        float proj = __fsub_rn(p.x, __fmul_rn(p.tau, __fadd_rn(p.c, aty)));
+        if (proj < p.l) proj = p.l;
+        if (proj > p.u) proj = p.u;
+        lmax = fmaxf(lmax, fabsf(__fsub_rn(p.x, proj)) / fmaxf(1e-4f, p.tau));
+    }
+};
+
 template <bool EXACT>
-__global__ void __launch_bounds__(256) plain_primal_kernel(SegMatrix At, SpmvPlan P, PlainVecs v,
+__global__ void __launch_bounds__(256, 8) plain_primal_kernel(SegMatrix At, SpmvPlan P, PlainVecs v,
                                                            const PlainState* __restrict__ st) {
     if (st->done) return;
-    auto epi = [&](int j, float aty) {
-        const float x_old = v.x[j];
-        const float grad = __fadd_rn(v.c[j], aty);
-        float x_new = __fsub_rn(x_old, __fmul_rn(v.tau[j], grad));
-        const float lo = v.l[j], up = v.u[j];
-        if (x_new < lo) x_new = lo;
-        if (x_new > up) x_new = up;
-        v.x[j] = x_new;
-        v.xbar[j] = __fsub_rn(__fmul_rn(2.0f, x_new), x_old);
-    };
+    PrimalEpi epi{v};
     spmv_run<EXACT>(At, P, v.y, epi);
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(256) plain_dual_kernel(SegMatrix A, SpmvPlan P, PlainVecs v,
+__global__ void __launch_bounds__(256, 8) plain_dual_kernel(SegMatrix A, SpmvPlan P, PlainVecs v,
                                                          const PlainState* __restrict__ st) {
     if (st->done) return;
-    auto epi = [&](int i, float axbar) {
-        const float sig = v.sigma[i];
-        const float w = __fadd_rn(axbar, v.y[i] / sig);
-        float p = w;
-        const float lo = v.rl[i], up = v.ru[i];
-        if (p < lo) p = lo;
-        if (p > up) p = up;
-        v.y[i] = __fmul_rn(sig, __fsub_rn(w, p));
-    };
+    DualEpi epi{v};
     spmv_run<EXACT>(A, P, v.xbar, epi);
 }
 
-// Row violations of A x (cuda_pdhg.cu:114-129), max-reduced on the device.
 template <bool EXACT>
-__global__ void __launch_bounds__(256) plain_check_rows_kernel(SegMatrix A, SpmvPlan P, PlainVecs v,
+__global__ void __launch_bounds__(256, 8) plain_check_rows_kernel(SegMatrix A, SpmvPlan P, PlainVecs v,
                                                                PlainState* st) {
     if (st->done) return;
     __shared__ float red[32];
-    float lmax = 0.f;
-    auto epi = [&](int i, float ax) {
-        const float lo = v.rl[i], up = v.ru[i];
-        float viol = 0.0f;
-        if (lo > -1e15f && ax < lo) viol = fmaxf(viol, __fsub_rn(lo, ax));
-        if (up < 1e15f && ax > up) viol = fmaxf(viol, __fsub_rn(ax, up));
-        lmax = fmaxf(lmax, viol);
-    };
+    RowViolEpi epi{v, 0.f};
     spmv_run<EXACT>(A, P, v.x, epi);
-    const float b = block_max_nonneg(lmax, red);
+    const float b = block_max_nonneg(epi.lmax, red);
     if (threadIdx.x == 0 && b > 0.f) atomicMax(&st->max_p_bits, __float_as_uint(b));
 }
 
-// Column measures |x - clip(x - tau (c + A^T y))| / max(1e-4, tau) (cuda_pdhg.cu:131-151).
-// NaN measures are skipped, as the reference's host std::max skips them.
 template <bool EXACT>
-__global__ void __launch_bounds__(256) plain_check_cols_kernel(SegMatrix At, SpmvPlan P, PlainVecs v,
+__global__ void __launch_bounds__(256, 8) plain_check_cols_kernel(SegMatrix At, SpmvPlan P, PlainVecs v,
                                                                PlainState* st) {
     if (st->done) return;
     __shared__ float red[32];
-    float lmax = 0.f;
-    auto epi = [&](int j, float aty) {
-        const float xj = v.x[j];
-        const float grad = __fadd_rn(v.c[j], aty);
-        const float step = v.tau[j];
-        float proj = __fsub_rn(xj, __fmul_rn(step, grad));
-        const float lo = v.l[j], up = v.u[j];
-        if (proj < lo) proj = lo;
-        if (proj > up) proj = up;
-        const float meas = fabsf(__fsub_rn(xj, proj)) / fmaxf(1e-4f, step);
-        lmax = fmaxf(lmax, meas);  // fmaxf drops a NaN operand
-    };
+    ColMeasEpi epi{v, 0.f};
     spmv_run<EXACT>(At, P, v.y, epi);
-    const float b = block_max_nonneg(lmax, red);
+    const float b = block_max_nonneg(epi.lmax, red);
     if (threadIdx.x == 0 && b > 0.f) atomicMax(&st->max_d_bits, __float_as_uint(b));
 }
 

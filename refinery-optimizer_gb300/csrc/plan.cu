@@ -5,6 +5,14 @@
 
 namespace sihg {
 
+// About kBatch entries per lane for a mean-length segment: one batch of
+// loads covers it.  Power of two in [1, 32].
+int default_lanes(double mean_len) {
+    int L = 1;
+    while (L < 32 && (double)(2 * L * kBatch) <= mean_len * 2.0) L *= 2;
+    return L;
+}
+
 SpmvPlan make_plan(const std::vector<int>& ptr, int lanes, int heavy_factor, bool exact, int sm_count,
                    std::vector<int>& heavy) {
     SpmvPlan P{};
@@ -21,13 +29,7 @@ SpmvPlan make_plan(const std::vector<int>& ptr, int lanes, int heavy_factor, boo
         P.light_blocks = std::max(1, std::min((nseg + P.threads - 1) / P.threads, sm_count * 8));
         return P;
     }
-    if (lanes <= 0) {
-        // lanes ~ mean segment length / 2, so that a light segment takes ~2
-        // entries per lane; power of two in [1, 32]
-        const double mean = nseg > 0 ? (double)nnz / nseg : 1.0;
-        lanes = 1;
-        while (lanes < 32 && 2.0 * lanes * 2.0 <= mean) lanes *= 2;
-    }
+    if (lanes <= 0) lanes = default_lanes(nseg > 0 ? (double)nnz / nseg : 1.0);
     lanes = std::max(1, std::min(32, lanes));
     while (lanes & (lanes - 1)) lanes &= lanes - 1;  // round down to a power of two
     if (heavy_factor <= 0) heavy_factor = 16;

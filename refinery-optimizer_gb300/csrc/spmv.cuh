@@ -2,22 +2,28 @@
 //
 // A "segment matrix" is one side of the LP matrix: the rows of A (CSR, used
 // for A x) or the columns of A (CSC, used for A^T y).  Entries are stored as
-// packed 8-byte pairs {index, float bits} so that one 64-bit load brings both
-// the index and the value of a nonzero (one load instruction and one 32-byte
-// sector per 4 nonzeros of a segment).
+// packed 8-byte pairs {index, float bits}: one 64-bit load brings the index and
+// the value of a nonzero.
 //
-// Work split (one launch):
-//   * light segments (length <= heavy_threshold) are handled by groups of
-//     `lanes` consecutive threads (1..32), in natural segment order, so the
-//     per-segment epilogue reads and writes its vectors coalesced;
-//   * heavy segments (longer) are listed in heavy_idx and handled by whole
-//     warps in the first `heavy_blocks` blocks of the grid.
-// The epilogue functor `epi(seg, dot)` runs once per segment on the lane that
-// owns the reduced dot product; it fuses the PDHG update of that row/column.
+// Memory-level parallelism is what bounds these kernels (two dependent loads
+// per nonzero: the pair, then the gathered vector element), so every lane
+// issues its loads in batches of U: U pair loads, then U gathers, then U FMAs,
+// with out-of-range slots predicated off.  The next segment's pointers and the
+// epilogue's own operands are loaded before the current dot product so their
+// latency overlaps it.
+//
+// Work split of the grid-stride form (plain path):
+//   * light segments (length <= heavy_threshold): groups of `lanes` threads,
+//     natural segment order (the epilogue's vector accesses stay coalesced);
+//   * heavy segments: listed in heavy_idx, one warp each, in the first
+//     heavy_blocks blocks of the grid.
+// The epilogue is a functor with
+//     using Pre = ...;  Pre pre(int seg);  void apply(int seg, float dot, const Pre&);
+// pre() loads the segment's operands, apply() performs the fused update.
 //
 // EXACT mode reproduces the reference kernels' arithmetic
-// (core/src/gpu/cuda_pdhg.cu:14-49): one thread per segment, products and
-// sums in entry order, no fused multiply-add.
+// (core/src/gpu/cuda_pdhg.cu:14-49): one thread per segment, products and sums
+// in entry order, no fused multiply-add.
 #pragma once
 
 #include "common.cuh"
@@ -41,6 +47,8 @@ struct SpmvPlan {
     int grid() const { return heavy_blocks + light_blocks; }
 };
 
+constexpr int kBatch = 4;  // loads in flight per lane per batch
+
 __device__ __forceinline__ int2 ld_pair(const int2* p) {
     int2 v;
     asm("ld.global.nc.L1::no_allocate.v2.s32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
@@ -49,25 +57,48 @@ __device__ __forceinline__ int2 ld_pair(const int2* p) {
 
 __device__ __forceinline__ float ld_vec(const float* p) { return __ldg(p); }
 
-// Dot product of one segment with `vec`, this lane's share: entries
-// beg + lane0, beg + lane0 + L, ...  (four independent loads in flight).
+// This lane's share of a segment dot product: entries beg+lane0, +L, +2L, ...
 __device__ __forceinline__ float seg_dot(const int2* __restrict__ pairs, int beg, int end, int lane0, int L,
                                          const float* __restrict__ vec) {
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-    int k = beg + lane0;
-    for (; k + 3 * L < end; k += 4 * L) {
-        const int2 p0 = ld_pair(pairs + k), p1 = ld_pair(pairs + k + L);
-        const int2 p2 = ld_pair(pairs + k + 2 * L), p3 = ld_pair(pairs + k + 3 * L);
-        s0 = fmaf(__int_as_float(p0.y), ld_vec(vec + p0.x), s0);
-        s1 = fmaf(__int_as_float(p1.y), ld_vec(vec + p1.x), s1);
-        s2 = fmaf(__int_as_float(p2.y), ld_vec(vec + p2.x), s2);
-        s3 = fmaf(__int_as_float(p3.y), ld_vec(vec + p3.x), s3);
+    float acc[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) acc[u] = 0.f;
+    for (int k = beg + lane0; k < end; k += kBatch * L) {
+        int2 p[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) p[u] = (k + u * L < end) ? ld_pair(pairs + k + u * L) : make_int2(0, 0);
+        float v[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) v[u] = (k + u * L < end) ? ld_vec(vec + p[u].x) : 0.f;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) acc[u] = fmaf(__int_as_float(p[u].y), v[u], acc[u]);
     }
-    for (; k < end; k += L) {
-        const int2 p0 = ld_pair(pairs + k);
-        s0 = fmaf(__int_as_float(p0.y), ld_vec(vec + p0.x), s0);
+    return (acc[0] + acc[1]) + (acc[2] + acc[3]);
+}
+
+// Compensated share (Ogita-Rump-Oishi Dot2): returns s and e with s + e equal
+// to this lane's partial dot product evaluated in about twice FP32 precision.
+__device__ __forceinline__ void seg_dot2(const int2* __restrict__ pairs, int beg, int end, int lane0, int L,
+                                         const float* __restrict__ vec, float& s_out, float& e_out) {
+    float s = 0.f, e = 0.f;
+    for (int k = beg + lane0; k < end; k += kBatch * L) {
+        int2 p[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) p[u] = (k + u * L < end) ? ld_pair(pairs + k + u * L) : make_int2(0, 0);
+        float v[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) v[u] = (k + u * L < end) ? ld_vec(vec + p[u].x) : 0.f;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+            float pr, pe, ss, se;
+            two_prod(__int_as_float(p[u].y), v[u], pr, pe);
+            two_sum(s, pr, ss, se);
+            s = ss;
+            e = __fadd_rn(e, __fadd_rn(pe, se));
+        }
     }
-    return (s0 + s1) + (s2 + s3);
+    s_out = s;
+    e_out = e;
 }
 
 // Reference-order dot: sum = sum + v * x, entry by entry, unfused.
@@ -81,57 +112,88 @@ __device__ __forceinline__ float seg_dot_exact(const int2* __restrict__ pairs, i
     return s;
 }
 
+// Sum over the L lanes of a group (lane 0 of the group gets the total).
+__device__ __forceinline__ float group_sum(float s, int L) {
+    for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_down_sync(FULL_MASK, s, o, L);
+    return s;
+}
+
+// Compensated group sum of (s, e) pairs.
+__device__ __forceinline__ void group_sum2(float& s, float& e, int L) {
+    for (int o = L >> 1; o > 0; o >>= 1) {
+        const float s2 = __shfl_down_sync(FULL_MASK, s, o, L);
+        const float e2 = __shfl_down_sync(FULL_MASK, e, o, L);
+        float t, te;
+        two_sum(s, s2, t, te);
+        s = t;
+        e = __fadd_rn(e, __fadd_rn(e2, te));
+    }
+}
+
+// Light segments [s0, s1) handled by groups of L lanes; this thread's group is
+// `group` of `ngroups` (group-strided).  Segments longer than `heavy_threshold`
+// are skipped (handled elsewhere).  Warp-uniform loop.
 template <bool EXACT, class Epi>
-__device__ __forceinline__ void spmv_light(const SegMatrix& A, const SpmvPlan& P, const float* __restrict__ vec,
-                                           int rank, int nblocks, Epi& epi) {
-    const int L = EXACT ? 1 : P.lanes;
-    const int lane = threadIdx.x & 31;
-    const int sub = lane & (L - 1);
-    const int gpw = 32 / L;
-    const int wpb = blockDim.x >> 5;
-    const int wid = rank * wpb + (threadIdx.x >> 5);
-    const int nw = nblocks * wpb;
-    for (int base = wid * gpw; base < A.nseg; base += nw * gpw) {
-        const int r = base + lane / L;
+__device__ __forceinline__ void spmv_groups(const SegMatrix& A, const float* __restrict__ vec, int s0, int s1,
+                                            int group, int ngroups, int L, int heavy_threshold, Epi& epi) {
+    const int sub = (threadIdx.x & 31) & (L - 1);
+    // first segment of this group; every lane of a warp runs the same trip count
+    int r = s0 + group;
+    const int warp_first = s0 + (group - (((threadIdx.x & 31)) / L));
+    int beg = 0, end = 0;
+    if (r < s1) {
+        beg = A.ptr[r];
+        end = A.ptr[r + 1];
+    }
+    for (int wbase = warp_first; wbase < s1; wbase += ngroups, r += ngroups) {
+        // prefetch the next segment's pointers
+        const int rn = r + ngroups;
+        int nbeg = 0, nend = 0;
+        if (rn < s1) {
+            nbeg = A.ptr[rn];
+            nend = A.ptr[rn + 1];
+        }
+        const bool active = r < s1 && (EXACT || (end - beg) <= heavy_threshold);
+        typename Epi::Pre pre{};
+        if (active && sub == 0) pre = epi.pre(r);
         float s = 0.f;
-        bool active = false;
-        if (r < A.nseg) {
-            const int beg = A.ptr[r], end = A.ptr[r + 1];
-            active = EXACT || (end - beg) <= P.heavy_threshold;
-            if (active) s = EXACT ? seg_dot_exact(A.pairs, beg, end, vec) : seg_dot(A.pairs, beg, end, sub, L, vec);
-        }
-        if (!EXACT) {
-            for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_down_sync(FULL_MASK, s, o, L);
-        }
-        if (active && sub == 0) epi(r, s);
+        if (active) s = EXACT ? seg_dot_exact(A.pairs, beg, end, vec) : seg_dot(A.pairs, beg, end, sub, L, vec);
+        if (!EXACT) s = group_sum(s, L);
+        if (active && sub == 0) epi.apply(r, s, pre);
+        beg = nbeg;
+        end = nend;
     }
 }
 
+// One segment per warp (heavy segments).
 template <class Epi>
-__device__ __forceinline__ void spmv_heavy(const SegMatrix& A, const SpmvPlan& P, const float* __restrict__ vec,
-                                           int rank, int nblocks, Epi& epi) {
+__device__ __forceinline__ void spmv_warp_seg(const SegMatrix& A, const float* __restrict__ vec, int r, Epi& epi) {
     const int lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    const int wid = rank * wpb + (threadIdx.x >> 5);
-    const int nw = nblocks * wpb;
-    for (int h = wid; h < P.heavy_count; h += nw) {
-        const int r = P.heavy_idx[h];
-        float s = seg_dot(A.pairs, A.ptr[r], A.ptr[r + 1], lane, 32, vec);
+    typename Epi::Pre pre{};
+    if (lane == 0) pre = epi.pre(r);
+    float s = seg_dot(A.pairs, A.ptr[r], A.ptr[r + 1], lane, 32, vec);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
-        if (lane == 0) epi(r, s);
-    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+    if (lane == 0) epi.apply(r, s, pre);
 }
 
-// Runs the whole SpMV of one launch: heavy blocks first, then light blocks.
+// Grid-stride SpMV of a whole side: heavy blocks first, then light blocks.
 template <bool EXACT, class Epi>
 __device__ __forceinline__ void spmv_run(const SegMatrix& A, const SpmvPlan& P, const float* __restrict__ vec,
                                          Epi& epi) {
-    if (!EXACT && (int)blockIdx.x < P.heavy_blocks)
-        spmv_heavy(A, P, vec, blockIdx.x, P.heavy_blocks, epi);
-    else
-        spmv_light<EXACT>(A, P, vec, blockIdx.x - (EXACT ? 0 : P.heavy_blocks),
-                          gridDim.x - (EXACT ? 0 : P.heavy_blocks), epi);
+    const int wpb = blockDim.x >> 5;
+    if (!EXACT && (int)blockIdx.x < P.heavy_blocks) {
+        const int nw = P.heavy_blocks * wpb;
+        for (int h = blockIdx.x * wpb + (threadIdx.x >> 5); h < P.heavy_count; h += nw)
+            spmv_warp_seg(A, vec, P.heavy_idx[h], epi);
+        return;
+    }
+    const int L = EXACT ? 1 : P.lanes;
+    const int rank = blockIdx.x - (EXACT ? 0 : P.heavy_blocks);
+    const int nblocks = gridDim.x - (EXACT ? 0 : P.heavy_blocks);
+    const int gpw = 32 / L;
+    const int group = (rank * wpb + (threadIdx.x >> 5)) * gpw + (threadIdx.x & 31) / L;
+    spmv_groups<EXACT>(A, vec, 0, A.nseg, group, nblocks * wpb * gpw, L, P.heavy_threshold, epi);
 }
 
 // ------------------------------------------------------------------ host side
@@ -140,5 +202,8 @@ __device__ __forceinline__ void spmv_run(const SegMatrix& A, const SpmvPlan& P, 
 // written to `heavy` (host vector) for the caller to upload.
 SpmvPlan make_plan(const std::vector<int>& ptr, int lanes, int heavy_factor, bool exact, int sm_count,
                    std::vector<int>& heavy);
+
+// Default lanes per segment for a mean segment length.
+int default_lanes(double mean_len);
 
 }  // namespace sihg

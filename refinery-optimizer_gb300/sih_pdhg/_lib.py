@@ -14,7 +14,7 @@ import numpy as np
 from .config import GpuPdhgConfig
 
 PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(PKG_DIR, "_build", "libsih_pdhg.so")
+LIB_PATH = os.environ.get("SIH_PDHG_LIB") or os.path.join(PKG_DIR, "_build", "libsih_pdhg.so")
 
 OK = 0
 ERR_NAMES = {1: "invalid argument", 2: "no CUDA device", 3: "CUDA error", 4: "out of memory", 5: "unsupported"}
@@ -45,7 +45,8 @@ class COptions(C.Structure):
                 ("verbose", C.c_int32), ("time_limit_sec", C.c_double), ("restart_sufficient", C.c_double),
                 ("restart_necessary", C.c_double), ("restart_artificial", C.c_double),
                 ("primal_weight_smoothing", C.c_double), ("exact_arithmetic", C.c_int32),
-                ("lanes_csr", C.c_int32), ("lanes_csc", C.c_int32), ("heavy_factor", C.c_int32)]
+                ("lanes_csr", C.c_int32), ("lanes_csc", C.c_int32), ("heavy_factor", C.c_int32),
+                ("tile_nnz", C.c_int32)]
 
 
 class CResult(C.Structure):
