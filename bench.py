@@ -1,0 +1,324 @@
+#!/usr/bin/env python3
+"""Benchmark: time to 1e-4 relative KKT of the GB300 PDHG engine.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl gb300|reference]
+
+One step = one complete solve of the workload LP from its initial point to
+relative KKT <= 1e-4 (primal, dual and gap, docs/gpu_pdhg.md:51-57 definitions)
+with the mixed-precision restarted adaptive PDHG, the problem already resident
+in HBM (handle API).  `value` is the mean device time of a step (CUDA events on
+the solver stream, max over ranks); `e2e` is the same solve through the C ABI
+entry point with host buffers (conversion, upload, scaling, solve, download and
+FP64 KKT packing inside the timed region).
+
+Workloads (seeded synthetic LPs, FP64 data, generators in sih_pdhg.generators):
+  zipf-500kx1m  m=500,000 (half equalities), n=1,000,000, 12M nonzeros, column
+                counts Zipf(1.5) clipped to [2, 2000] and rescaled (default)
+  random-2kx5k  m=2,000, n=5,000, 8 nonzeros per column
+
+Multi-GPU: replicas (each rank solves its own copy; scaling "weak").
+--impl reference times the reference's algorithm (plain FP32 PDHG) through its
+CPU port (oracle/pdhg_oracle.c, OpenMP over all host threads) on a bounded
+sample of iterations, scaled by the iterations that algorithm needs to reach
+the same tolerance on the same LP.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "refinery-optimizer_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "time-to-1e-4 rel. KKT & HBM GB/s: batched mixed vs plain PDHG, 1×GB300"
+
+# Iterations the plain reference algorithm (FP32 PDHG, fixed diagonal steps,
+# gpu_solver.cpp:128-151) needs on each workload before its best iterate and
+# last dual reach relative KKT <= 1e-4: the first point of a measured grid at
+# or below the tolerance (this engine's plain path, same iterates as the
+# reference up to FP32 summation order).  zipf-500kx1m: 14,000 iterations give
+# a relative gap of 1.007e-4, 16,000 give 8.3e-5; random-2kx5k: 8,000 give
+# 1.08e-4, 12,000 give 5.3e-5.
+PLAIN_ITERS_TO_TOL = {
+    "zipf-500kx1m": 16000,
+    "random-2kx5k": 12000,
+}
+PLAIN_ITERS_LOWER_BOUND = {
+    "zipf-500kx1m": 200000,
+    "random-2kx5k": 20000,
+}
+
+# DRAM bytes per launch of the dominant kernel, read from one ncu capture of
+# the same kernel on the same workload (dram__bytes_read.sum + write.sum);
+# profiles/ holds the capture summary.  None until captured.
+NCU_TRAFFIC_PER_LAUNCH = {}
+
+
+def make_workload(name: str, seed: int = 0):
+    from sih_pdhg.generators import small_random_lp, zipf_lp
+
+    if name == "zipf-500kx1m":
+        return zipf_lp(500_000, 1_000_000, 12_000_000, seed)
+    if name == "random-2kx5k":
+        return small_random_lp(2000, 5000, 8, seed)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="zipf-500kx1m", choices=["zipf-500kx1m", "random-2kx5k"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--tol", type=float, default=1e-4)
+    ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+# ------------------------------------------------------------------ clocks
+CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.path = tempfile.mktemp(prefix="clocks_", suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={CLOCK_QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_hbm_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU baselines (oracle = test/baseline only)
+def cpu_pdlp_sample(problem, gpu_attempts: int, budget_s: float) -> dict:
+    """FP64 CPU port of the same mixed algorithm (oracle/pdlp_oracle.c, one
+    thread) on a bounded number of steps, scaled to the GPU's step count."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    oracle.build()
+    attempts = 64
+    t0 = time.perf_counter()
+    oracle.pdlp_solve(problem, max_attempts=attempts, tol=1e-30)
+    dt = time.perf_counter() - t0
+    while dt < budget_s / 3 and attempts < 4096:
+        attempts *= 2
+        t0 = time.perf_counter()
+        oracle.pdlp_solve(problem, max_attempts=attempts, tol=1e-30)
+        dt = time.perf_counter() - t0
+    per_step = dt / attempts  # includes scaling and evaluations, amortised
+    return {"value": per_step * gpu_attempts, "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"{attempts} steps of the FP64 CPU port of the same algorithm ({dt:.1f} s), "
+                      f"scaled to the {gpu_attempts} steps the GPU needed"}
+
+
+def cpu_plain_per_iteration(data, iters: int, threads: int) -> float:
+    """Seconds per iteration of the reference algorithm's CPU port
+    (oracle_plain_iterations: the four reference kernels, OpenMP) on arrays
+    prepared once by oracle.plain_prepare."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    t0 = time.perf_counter()
+    oracle.plain_iterations(data, iters, threads)
+    return (time.perf_counter() - t0) / iters
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    prob = make_workload(args.workload)
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    oracle.build()
+    data = oracle.plain_prepare(prob)
+    its_needed = PLAIN_ITERS_TO_TOL.get(args.workload)
+    lower = its_needed is None
+    if lower:
+        its_needed = PLAIN_ITERS_LOWER_BOUND[args.workload]
+    # each step: a bounded sample of iterations sized to ~2 s
+    probe = cpu_plain_per_iteration(data, 3, threads)
+    sample = max(3, int(2.0 / max(probe, 1e-6)))
+    for _ in range(args.warmup):
+        cpu_plain_per_iteration(data, max(3, sample // 4), threads)
+    ests = []
+    for _ in range(args.steps):
+        ests.append(cpu_plain_per_iteration(data, sample, threads) * its_needed)
+    value = statistics.mean(ests)
+    note = (f"{sample} iterations of the reference algorithm's CPU port per step, x {its_needed} iterations "
+            + ("(lower bound: the plain algorithm did not reach the tolerance within this many)" if lower else
+               "needed to reach the tolerance"))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, seed 0)",
+            "config": {"workload": args.workload, "m": prob.num_rows(), "n": prob.num_cols(),
+                       "nnz": prob.num_nonzeros(), "tol": args.tol, "algorithm": "plain FP32 PDHG (reference)"},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": note},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GB300 arm
+def run_gb300(args) -> None:
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import sih_pdhg
+
+    if not sih_pdhg.GpuSolver.is_cuda_available():
+        raise SystemExit("bench.py needs a CUDA device")
+    torch.cuda.set_device(local)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v: float) -> float:
+        if world == 1:
+            return v
+        import torch.distributed as dist
+
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    prob = make_workload(args.workload, seed=0)
+    tol = args.tol
+    cfg = sih_pdhg.GpuPdhgConfig(max_iterations=1_000_000, tol_primal=tol, tol_dual=tol, tol_gap=tol)
+    handle = sih_pdhg.PdhgHandle(prob, cfg, algorithm=sih_pdhg.ALGO_MIXED)
+    for _ in range(args.warmup):
+        handle.run()
+    barrier()
+    clocks = ClockSampler(local)
+    times = []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        times.append(handle.run())
+    barrier()
+    wall = time.perf_counter() - t_wall
+    clock_info = clocks.stop()
+    sol = handle.result(0)
+    step = max_over_ranks(statistics.mean(times))
+    launches = sol.kernel_launches * args.steps
+
+    # roofline of the dominant SpMV kernel (live CUDA-event timing on the solver stream)
+    secs, byts = handle.time_kernels(20)
+    names = ["k_step_primal", "k_step_dual", "k_step_kty"]
+    dom = max(range(3), key=lambda k: secs[k])
+    peak, peak_src = measured_hbm_peak()
+    achieved = byts[dom] / secs[dom] / 1e9
+    all_gbs = {names[k]: round(byts[k] / secs[k] / 1e9, 1) for k in range(3)}
+    handle.close()
+
+    # end to end through the C ABI with host buffers (upload .. download inside)
+    e2e_times = []
+    e2e_sol = None
+    for i in range(2):
+        barrier()
+        t0 = time.perf_counter()
+        e2e_sol = sih_pdhg.solve_gpu_mixed(prob, cfg)
+        torch.cuda.synchronize()
+        if i > 0 or args.steps <= 1:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e = max_over_ranks(statistics.mean(e2e_times))
+
+    if rank != 0:
+        return
+    m, n, nnz = prob.num_rows(), prob.num_cols(), prob.num_nonzeros()
+    plain_its = PLAIN_ITERS_TO_TOL.get(args.workload)
+    line = {
+        "metric": METRIC, "value": step, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded generator, seed 0)",
+        "config": {"workload": args.workload, "m": m, "n": n, "nnz": nnz, "tol": tol,
+                   "algorithm": "mixed-precision restarted adaptive PDHG", "parallelism": f"replicas x{world}",
+                   "l2": "working set ~300 MB > 129 MB L2 (no flush needed)"},
+        "iterations": sol.simplex_iterations, "restarts": sol.restarts, "status": int(sol.status),
+        "rel_kkt": [sol.rel_primal, sol.rel_dual, sol.rel_gap], "wall_s_per_step": wall / args.steps,
+        "clocks": clock_info,
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(e2e_sol.h2d_bytes),
+                "d2h_bytes_per_step": int(e2e_sol.d2h_bytes)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                     "traffic": NCU_TRAFFIC_PER_LAUNCH.get((args.workload, names[dom])),
+                     "algorithmic_bytes_per_launch": byts[dom], "all_kernels_gbs": all_gbs},
+        "plain_reference_iterations_to_tol": plain_its,
+    }
+    line["cpu_baseline"] = cpu_pdlp_sample(prob, sol.simplex_iterations, args.cpu_sample_seconds)
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -153,7 +153,13 @@ typedef struct sih_pdhg_result {
     int64_t step_rejections;
     double final_step;
     double final_primal_weight;
+    uint64_t h2d_bytes;     /* host -> device bytes this solve moved (problem upload, start point) */
+    uint64_t d2h_bytes;     /* device -> host bytes this solve moved (returned point, status) */
+    uint64_t kernel_launches; /* kernels this solve launched (graph nodes counted one by one) */
 } sih_pdhg_result;
+
+/* Opaque solver handle: one LP or a batch of LPs resident on the device. */
+typedef struct sih_pdhg_handle sih_pdhg_handle;
 
 /* ---- metadata ----------------------------------------------------------- */
 int sih_pdhg_abi_version(void);
@@ -184,6 +190,36 @@ int sih_pdhg_solve(const sih_pdhg_problem* problem, const sih_pdhg_config* confi
 /* sih_pdhg_solve with the added options (algorithm choice etc.).  opts may be NULL (defaults). */
 int sih_pdhg_solve_ex(const sih_pdhg_problem* problem, const sih_pdhg_config* config,
                       const sih_pdhg_options* opts, sih_pdhg_result* result);
+
+/* ---- handle API (problems resident on the device between solves) --------
+ * Added entry points with no single counterpart in the reference, which
+ * re-uploads the problem on every solve_pdhg call (gpu_solver.cpp:153-216). */
+
+/* Uploads `count` LPs (count >= 1) and prepares them for `opts->algorithm`:
+ * mixed = one block-diagonal batch solved by one set of kernels with
+ * per-instance state; plain = `count` reference-semantics solvers run one
+ * after another.  The problem arrays must stay valid until
+ * sih_pdhg_destroy (results are checked against them in FP64). */
+int sih_pdhg_create(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
+                    const sih_pdhg_options* opts, sih_pdhg_handle** out);
+/* Solves every instance from its initial point; iterates stay on the device.
+ * Returns after all instances stopped.  *device_seconds (may be NULL) gets the
+ * device time of the solve (CUDA events on the handle's stream). */
+int sih_pdhg_run(sih_pdhg_handle* h, double* device_seconds);
+/* Copies instance `index`'s returned point to the host and fills *result
+ * (FP64 KKT packing against the problem data given at creation). */
+int sih_pdhg_get_result(sih_pdhg_handle* h, int32_t index, sih_pdhg_result* result);
+/* Times `reps` back-to-back launches of each SpMV kernel of the mixed solver
+ * with CUDA events on the handle's stream: seconds[0] the elementwise primal
+ * step, [1] the A x step (rows), [2] the A^T y step (columns); bytes[0..2] get
+ * each kernel's algorithmic bytes per launch.  The state is reset by the next run. */
+int sih_pdhg_time_kernels(sih_pdhg_handle* h, int32_t reps, double* seconds, double* bytes);
+void sih_pdhg_destroy(sih_pdhg_handle* h);
+
+/* One-call batch: create + run + result for each instance + destroy.
+ * results[count] (arrays inside each may be NULL). */
+int sih_pdhg_solve_batch(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
+                         const sih_pdhg_options* opts, sih_pdhg_result* results);
 
 /* ---- kernel launchers (device pointers, int32 indices, float values) -----
  * Same arguments and results as the reference's launchers; the reference

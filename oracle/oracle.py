@@ -167,3 +167,38 @@ def pdlp_solve(problem, max_attempts=100000, tol=1e-4, tol_p=None, tol_d=None, t
                             _p(problem.row_upper, C.c_double), C.byref(o), _p(x, C.c_double), _p(y, C.c_double),
                             C.byref(info))
     return x, y, {k: getattr(info, k) for k, _ in PdlpInfo._fields_}
+
+
+def plain_prepare(problem):
+    """FP32/int32 arrays of the reference algorithm for oracle_plain_iterations
+    (the CPU baseline's timing loop).  Step sizes 0.95 / max(1, sum |a|) as in
+    gpu_solver.cpp:128-151 (summed by numpy here: the sample is a timing sample)."""
+    A = problem.A
+    m, n = problem.num_rows(), problem.num_cols()
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    cp, ri, cv = i32(A.csc_col_ptr()), i32(A.csc_row_ind()), f32(A.csc_values())
+    rp, ci, rv = i32(A.csr_row_ptr()), i32(A.csr_col_ind()), f32(A.csr_values())
+    cols = np.repeat(np.arange(n), np.diff(cp))
+    rows = np.repeat(np.arange(m), np.diff(rp))
+    colsum = np.bincount(cols, weights=np.abs(cv), minlength=n).astype(np.float32)
+    rowsum = np.bincount(rows, weights=np.abs(rv), minlength=m).astype(np.float32)
+    l, u = f32(problem.col_lower), f32(problem.col_upper)
+    x = np.maximum(l, np.minimum(u, np.float32(0)))
+    return dict(m=m, n=n, cp=cp, ri=ri, cv=cv, rp=rp, ci=ci, rv=rv, c=f32(problem.c), l=l, u=u,
+                rl=f32(problem.row_lower), ru=f32(problem.row_upper),
+                tau=(np.float32(0.95) / np.maximum(np.float32(1), colsum)).astype(np.float32),
+                sigma=(np.float32(0.95) / np.maximum(np.float32(1), rowsum)).astype(np.float32),
+                x=x.copy(), xbar=x.copy(), y=np.zeros(m, np.float32), aty=np.zeros(n, np.float32),
+                axbar=np.zeros(m, np.float32))
+
+
+def plain_iterations(d, iters: int, threads: int = 0) -> None:
+    """Runs `iters` reference PDHG iterations (the four kernels of
+    core/src/gpu/cuda_pdhg.cu:14-103, OpenMP) on prepared arrays, in place."""
+    F, I = C.c_float, C.c_int
+    lib().oracle_plain_iterations(
+        C.c_int(d["m"]), C.c_int(d["n"]), _p(d["cp"], I), _p(d["ri"], I), _p(d["cv"], F), _p(d["rp"], I),
+        _p(d["ci"], I), _p(d["rv"], F), _p(d["c"], F), _p(d["l"], F), _p(d["u"], F), _p(d["rl"], F),
+        _p(d["ru"], F), _p(d["tau"], F), _p(d["sigma"], F), _p(d["x"], F), _p(d["xbar"], F), _p(d["y"], F),
+        _p(d["aty"], F), _p(d["axbar"], F), C.c_int(iters), C.c_int(threads))

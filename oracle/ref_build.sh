@@ -10,6 +10,11 @@
 #                                    on the CPU; int64 index copies converted
 #                                    to int32 (the intended gpu_solver.cpp:202-203)
 #   oracle/_ref/faithful/_core*.so   same, with the shipped byte-for-byte copy
+#   oracle/_ref/engine/_core*.so     the reference pybind module with gpu_solver.cpp
+#                                    replaced by refinery-optimizer_gb300/host/
+#                                    gpu_solver_adapter.cpp, linked to the engine's
+#                                    libsih_pdhg.so (the drop-in, built when that
+#                                    library exists)
 #
 # The CUDA runtime is replaced by oracle/ref_emul/cuda_runtime.h and the kernel
 # launch syntax by oracle/ref_emul/ref_launchers.cpp.  Nothing else is
@@ -57,4 +62,13 @@ for variant in intended faithful; do
     wait
     $CXX -shared -fopenmp -o "$vo/_core$EXT" "$OUT"/obj/*.o "$vo/gpu_solver.o" "$vo/ref_launchers.o"
 done
+ENGINE_LIB="$HERE/../refinery-optimizer_gb300/_build"
+if [ -f "$ENGINE_LIB/libsih_pdhg.so" ]; then
+    mkdir -p "$OUT/engine"
+    $CXX $FLAGS -I"$HERE/../include" -c "$HERE/../refinery-optimizer_gb300/host/gpu_solver_adapter.cpp" \
+        -o "$OUT/engine/gpu_solver_adapter.o"
+    $CXX -shared -fopenmp -o "$OUT/engine/_core$EXT" "$OUT"/obj/*.o "$OUT/engine/gpu_solver_adapter.o" \
+        -L"$ENGINE_LIB" -lsih_pdhg -Wl,-rpath,"$ENGINE_LIB"
+    echo "ref_build: built $OUT/engine/_core$EXT (reference bindings over the engine)"
+fi
 echo "ref_build: built $OUT/intended/_core$EXT and $OUT/faithful/_core$EXT"

@@ -13,12 +13,12 @@ namespace sihg {
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 
-static bool device_present() {
+bool device_present() {
     int count = 0;
     return cudaGetDeviceCount(&count) == cudaSuccess && count > 0;
 }
 
-static void clear_result_scalars(sih_pdhg_result* r) {
+void clear_result_scalars(sih_pdhg_result* r) {
     r->status = SIH_STATUS_UNKNOWN;
     r->reserved0 = 0;
     r->iterations = 0;
@@ -28,7 +28,24 @@ static void clear_result_scalars(sih_pdhg_result* r) {
     r->time_wall_sec = r->time_solver_sec = 0.0;
     r->restarts = r->step_rejections = 0;
     r->final_step = r->final_primal_weight = 0.0;
+    r->h2d_bytes = r->d2h_bytes = 0;
+    r->kernel_launches = 0;
 }
+
+// Options of an entry point: defaults, or the caller's after a size check.
+int resolve_options(const sih_pdhg_options* in, sih_pdhg_options& out) {
+    sih_pdhg_options_default(&out);
+    if (in) {
+        if (in->struct_size != (int32_t)sizeof(sih_pdhg_options))
+            return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "options.struct_size does not match this library");
+        out = *in;
+    }
+    if (out.algorithm != SIH_PDHG_ALGO_PLAIN && out.algorithm != SIH_PDHG_ALGO_MIXED)
+        return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "unknown algorithm");
+    return SIH_PDHG_OK;
+}
+
+uint64_t instance_h2d_bytes(const HostProblem& p);
 
 // Fills the vectors and KKT fields of `r` from an FP64 primal/dual pair of
 // the internal (minimization) problem; y is in the PDHG sign.
@@ -55,11 +72,8 @@ void pack_solution(const sih_pdhg_problem* p, const sih_pdhg_options& opts, cons
     if (!finite) r->status = SIH_STATUS_NUMERICAL_FAILURE;
 }
 
-static int solve_plain(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
-                       sih_pdhg_result* r) {
-    PlainSolver solver;
-    SIHG_TRY(solver.setup(hp, cfg, opts));
-    SIHG_TRY(solver.iterate());
+// Packs the result of a plain solver that has iterated.
+int solve_plain_packed(PlainSolver& solver, const HostProblem& hp, const sih_pdhg_options& opts, sih_pdhg_result* r) {
     std::vector<float> xf, yf;
     SIHG_TRY(solver.fetch(xf, yf));
     std::vector<double> x(xf.begin(), xf.end()), y(yf.begin(), yf.end());
@@ -68,7 +82,19 @@ static int solve_plain(const HostProblem& hp, const sih_pdhg_config& cfg, const 
     r->ref_primal = solver.last_norm_p();
     r->ref_dual = solver.last_norm_d();
     r->time_solver_sec = solver.loop_seconds();
+    r->kernel_launches = solver.launches();
     pack_solution(hp.src, opts, x, y, r);
+    r->d2h_bytes = 4ull * (hp.n + hp.m);
+    return SIH_PDHG_OK;
+}
+
+static int solve_plain(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
+                       sih_pdhg_result* r) {
+    PlainSolver solver;
+    SIHG_TRY(solver.setup(hp, cfg, opts));
+    SIHG_TRY(solver.iterate());
+    SIHG_TRY(solve_plain_packed(solver, hp, opts, r));
+    r->h2d_bytes = instance_h2d_bytes(hp);
     return SIH_PDHG_OK;
 }
 
@@ -137,14 +163,7 @@ int sih_pdhg_solve_ex(const sih_pdhg_problem* problem, const sih_pdhg_config* co
     if (!result) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "result is NULL");
     clear_result_scalars(result);
     sih_pdhg_options opts;
-    sih_pdhg_options_default(&opts);
-    if (opts_in) {
-        if (opts_in->struct_size != (int32_t)sizeof(sih_pdhg_options))
-            return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "options.struct_size does not match this library");
-        opts = *opts_in;
-    }
-    if (opts.algorithm != SIH_PDHG_ALGO_PLAIN && opts.algorithm != SIH_PDHG_ALGO_MIXED)
-        return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "unknown algorithm");
+    SIHG_TRY(resolve_options(opts_in, opts));
     SIHG_TRY(validate_config(config));
     HostProblem hp;
     SIHG_TRY(build_host_problem(problem, hp));  // validates sizes, pointers and every index

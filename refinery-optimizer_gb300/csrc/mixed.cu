@@ -37,6 +37,8 @@
 
 namespace sihg {
 
+uint64_t instance_h2d_bytes(const HostProblem& p);
+
 // ---------------------------------------------------------------- helpers
 __device__ __forceinline__ float* pick(float* a, float* b, int sel) { return sel ? b : a; }
 __device__ __forceinline__ bool fin(float v) { return !isinf(v); }
@@ -870,6 +872,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
 }
 
 int MixedSolver::launch_step(cudaStream_t s) {
+    launches_ += 3;
     Inst* st = state_.as<Inst>();
     k_step_primal<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
     k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
@@ -879,6 +882,7 @@ int MixedSolver::launch_step(cudaStream_t s) {
 }
 
 int MixedSolver::launch_eval(cudaStream_t s) {
+    launches_ += 4;
     Inst* st = state_.as<Inst>();
     k_flush_avg<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
     k_eval_rows<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
@@ -906,6 +910,7 @@ int MixedSolver::reset_state() {
     }
     SIHG_CUDA(cudaMemcpyAsync(state_.as<Inst>(), host_inst_.data(), sizeof(Inst) * B_, cudaMemcpyHostToDevice, s));
     SIHG_CUDA(cudaMemsetAsync(done_count_.as<void>(), 0, sizeof(unsigned), s));
+    launches_ += 5;
     // initial point x = clip(0, l~, u~), y = 0; averages and last points equal it
     k_init_point<<<g, 256, 0, s>>>(N_, M_, V_);
     SIHG_LAUNCH_CHECK();
@@ -921,6 +926,7 @@ int MixedSolver::reset_state() {
 
 int MixedSolver::record_graph() {
     if (graphs_[0]) return SIH_PDHG_OK;
+    const unsigned long long saved = launches_;
     cudaGraph_t g = nullptr;
     SIHG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     int rc = SIH_PDHG_OK;
@@ -934,6 +940,7 @@ int MixedSolver::record_graph() {
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
     e = cudaGraphInstantiate(&graphs_[0], g, 0);
     cudaGraphDestroy(g);
+    launches_ = saved;  // capturing launches nothing
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __FILE__, __LINE__);
     return SIH_PDHG_OK;
 }
@@ -942,6 +949,7 @@ int MixedSolver::run() {
     eval_freq_ = opts_.eval_frequency > 0 ? opts_.eval_frequency : 64;
     if (opts_.use_graph) SIHG_TRY(record_graph());
     const auto t0 = std::chrono::steady_clock::now();
+    launches_ = 0;
     SIHG_TRY(reset_state());
     cudaStream_t s = stream_;
     constexpr int kWindow = 3;
@@ -973,6 +981,7 @@ int MixedSolver::run() {
             if (opts_.use_graph) {
                 cudaError_t e = cudaGraphLaunch(graphs_[0], s);
                 if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
+                launches_ += 3ull * eval_freq_ + 4ull;
             } else {
                 for (int k = 0; k < eval_freq_ && rc == SIH_PDHG_OK; ++k) rc = launch_step(s);
                 if (rc == SIH_PDHG_OK) rc = launch_eval(s);
@@ -1012,6 +1021,40 @@ int MixedSolver::fetch(int b, std::vector<double>& x, std::vector<double>& y) {
     return SIH_PDHG_OK;
 }
 
+int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
+    SIHG_TRY(reset_state());
+    cudaStream_t s = stream_;
+    Inst* st = state_.as<Inst>();
+    cudaEvent_t e0, e1;
+    SIHG_CUDA(cudaEventCreate(&e0));
+    SIHG_CUDA(cudaEventCreate(&e1));
+    int rc = SIH_PDHG_OK;
+    for (int k = 0; k < 3 && rc == SIH_PDHG_OK; ++k) {
+        cudaEventRecord(e0, s);
+        for (int i = 0; i < reps; ++i) {
+            if (k == 0) k_step_primal<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
+            if (k == 1) k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
+            if (k == 2) k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
+        }
+        cudaEventRecord(e1, s);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) rc = cuda_fail(e, "kernel timing", __FILE__, __LINE__);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        seconds[k] = ms * 1e-3 / reps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (bytes) {
+        // algorithmic bytes of one launch: every array the kernel must touch, once
+        const double nnz = (double)nnz_, m = M_, n = N_;
+        bytes[0] = 40.0 * n + 20.0 * m;                   // x,K^T y,c,l,u in, x' out, x/y averages in+out
+        bytes[1] = 8.0 * nnz + 4.0 * (m + 1) + 4.0 * n + 28.0 * m;  // pairs, ptr, x' gathered, row epilogue
+        bytes[2] = 8.0 * nnz + 4.0 * (n + 1) + 4.0 * m + 16.0 * n;  // pairs, ptr, y' gathered, column epilogue
+    }
+    return rc;
+}
+
 int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
                 sih_pdhg_result* r) {
     MixedSolver solver;
@@ -1022,6 +1065,8 @@ int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdh
     SIHG_TRY(solver.fetch(0, x, y));
     solver.fill_result(0, r);
     pack_solution(hp.src, opts, x, y, r);
+    r->d2h_bytes = 8ull * (hp.n + hp.m);
+    r->h2d_bytes = instance_h2d_bytes(hp);
     return SIH_PDHG_OK;
 }
 
@@ -1041,6 +1086,7 @@ void MixedSolver::fill_result(int b, sih_pdhg_result* r) const {
     r->ref_primal = S.rel_p[S.out_sel];
     r->ref_dual = S.rel_d[S.out_sel];
     r->time_solver_sec = loop_seconds_;
+    r->kernel_launches = launches_;
 }
 
 }  // namespace sihg

@@ -121,6 +121,8 @@ class MixedSolver {
     const Inst& inst(int b) const { return host_inst_[b]; }
     int launch_step(cudaStream_t s);
     int launch_eval(cudaStream_t s);
+    // Times `reps` launches of each step kernel (elementwise, rows, columns).
+    int time_kernels(int reps, double* seconds, double* bytes);
     long long nnz() const { return nnz_; }
     int rows() const { return M_; }
     int cols() const { return N_; }
@@ -140,6 +142,7 @@ class MixedSolver {
     int grid_ = 1;
     bool timed_out_ = false;
     double loop_seconds_ = 0.0;
+    unsigned long long launches_ = 0;  // kernels launched by the last run()
     cudaStream_t stream_ = nullptr;
     cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;
     cudaGraphExec_t graphs_[1] = {nullptr};

@@ -354,6 +354,7 @@ int PlainSolver::iterate() {
         cudaError_t e = cudaEventCreateWithFlags(&ev[w], cudaEventDisableTiming);
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate", __FILE__, __LINE__);
     }
+    launches_ = 0;
     if (rc == SIH_PDHG_OK) {
         cudaStream_t s = stream_;
         cudaEventRecord(ev_start_, s);
@@ -366,6 +367,7 @@ int PlainSolver::iterate() {
                 if (h_done[slot]) { done = true; break; }
             }
             const bool is_tail = b == nblocks;
+            launches_ += 2ull * (is_tail ? tail : cf) + 4ull;
             if (opts_.use_graph) {
                 cudaError_t e = cudaGraphLaunch(is_tail ? tail_exec_ : block_exec_, s);
                 if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }

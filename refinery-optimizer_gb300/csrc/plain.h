@@ -54,6 +54,7 @@ class PlainSolver {
     float last_norm_p() const { return host_state_.last_norm_p; }
     float last_norm_d() const { return host_state_.last_norm_d; }
     double loop_seconds() const { return loop_seconds_; }
+    unsigned long long launches() const { return launches_; }
     cudaStream_t stream() const { return stream_; }
     int launch_iteration(cudaStream_t s);
     int launch_check(cudaStream_t s);
@@ -80,6 +81,7 @@ class PlainSolver {
     std::vector<float> x0_;
     float max_abs_b_ = 1.f, max_abs_c_ = 1.f;
     double loop_seconds_ = 0.0;
+    unsigned long long launches_ = 0;  // kernels launched by the last iterate()
     PlainState host_state_{};
 };
 

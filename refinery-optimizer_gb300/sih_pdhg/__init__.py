@@ -21,8 +21,8 @@ from .config import GpuPdhgConfig
 from .problem import INF, ObjectiveSense, Problem, Solution, SolutionStatus, SparseMatrix
 
 __all__ = ["GpuSolver", "GpuPdhgConfig", "GpuMemoryInfo", "Problem", "SparseMatrix", "Solution",
-           "SolutionStatus", "ObjectiveSense", "solve_gpu_pdhg", "solve_gpu_mixed", "default_options",
-           "SihPdhgError", "ALGO_PLAIN", "ALGO_MIXED", "INF"]
+           "SolutionStatus", "ObjectiveSense", "solve_gpu_pdhg", "solve_gpu_mixed", "solve_batch", "PdhgHandle",
+           "default_options", "SihPdhgError", "ALGO_PLAIN", "ALGO_MIXED", "INF"]
 
 
 @dataclass
@@ -33,28 +33,107 @@ class GpuMemoryInfo:
     used_bytes: int = 0
 
 
+def _result_buffers(problem: Problem):
+    m, n = problem.num_rows(), problem.num_cols()
+    bufs = dict(x=np.zeros(n), row_duals=np.zeros(m), slack=np.zeros(m), reduced_costs=np.zeros(n))
+    res = _lib.CResult()
+    res.x, res.row_duals = bufs["x"].ctypes.data, bufs["row_duals"].ctypes.data
+    res.slack, res.reduced_costs = bufs["slack"].ctypes.data, bufs["reduced_costs"].ctypes.data
+    return res, bufs
+
+
+def _to_solution(res, bufs) -> Solution:
+    sol = Solution(status=SolutionStatus(res.status), primal_objective=res.primal_objective,
+                   dual_bound=res.dual_bound, simplex_iterations=int(res.iterations),
+                   time_wall_sec=res.time_wall_sec, time_solver_sec=res.time_solver_sec,
+                   rel_primal=res.rel_primal, rel_dual=res.rel_dual, rel_gap=res.rel_gap,
+                   ref_primal=res.ref_primal, ref_dual=res.ref_dual, restarts=int(res.restarts),
+                   step_rejections=int(res.step_rejections), final_step=res.final_step,
+                   final_primal_weight=res.final_primal_weight, **bufs)
+    sol.h2d_bytes = int(res.h2d_bytes)
+    sol.d2h_bytes = int(res.d2h_bytes)
+    sol.kernel_launches = int(res.kernel_launches)
+    return sol
+
+
 def _solve(problem: Problem, config: GpuPdhgConfig, opts) -> Solution:
     lib = _lib.load()
-    m, n = problem.num_rows(), problem.num_cols()
-    x = np.zeros(n)
-    y = np.zeros(m)
-    slack = np.zeros(m)
-    rc = np.zeros(n)
     cp, keep = _lib.c_problem(problem)
-    res = _lib.CResult()
-    res.x, res.row_duals, res.slack, res.reduced_costs = x.ctypes.data, y.ctypes.data, slack.ctypes.data, rc.ctypes.data
+    res, bufs = _result_buffers(problem)
     if opts is None:
         _lib.check(lib.sih_pdhg_solve(C.byref(cp), C.byref(config), C.byref(res)))
     else:
         _lib.check(lib.sih_pdhg_solve_ex(C.byref(cp), C.byref(config), C.byref(opts), C.byref(res)))
     del keep
-    return Solution(status=SolutionStatus(res.status), x=x, slack=slack, row_duals=y, reduced_costs=rc,
-                    primal_objective=res.primal_objective, dual_bound=res.dual_bound,
-                    simplex_iterations=int(res.iterations), time_wall_sec=res.time_wall_sec,
-                    time_solver_sec=res.time_solver_sec, rel_primal=res.rel_primal, rel_dual=res.rel_dual,
-                    rel_gap=res.rel_gap, ref_primal=res.ref_primal, ref_dual=res.ref_dual,
-                    restarts=int(res.restarts), step_rejections=int(res.step_rejections),
-                    final_step=res.final_step, final_primal_weight=res.final_primal_weight)
+    return _to_solution(res, bufs)
+
+
+class PdhgHandle:
+    """One LP or a batch of LPs kept resident on the GPU (sih_pdhg_create / run /
+    get_result / destroy).  The problems must outlive the handle."""
+
+    def __init__(self, problems, config: Optional[GpuPdhgConfig] = None, **options):
+        self._lib = _lib.load()
+        self.problems = list(problems) if isinstance(problems, (list, tuple)) else [problems]
+        self.config = config if config is not None else GpuPdhgConfig()
+        self.options = default_options(**options)
+        views = [_lib.c_problem(p) for p in self.problems]
+        self._keep = [v[1] for v in views]
+        arr = (_lib.CProblem * len(views))(*[v[0] for v in views])
+        self._arr = arr
+        h = C.c_void_p()
+        _lib.check(self._lib.sih_pdhg_create(arr, len(views), C.byref(self.config), C.byref(self.options),
+                                             C.byref(h)))
+        self._h = h
+
+    def run(self) -> float:
+        """Solves every instance from its initial point; returns the device seconds."""
+        secs = C.c_double()
+        _lib.check(self._lib.sih_pdhg_run(self._h, C.byref(secs)))
+        return secs.value
+
+    def result(self, index: int = 0) -> Solution:
+        if not 0 <= index < len(self.problems):
+            raise SihPdhgError(1, f"index {index} out of range")
+        res, bufs = _result_buffers(self.problems[index])
+        _lib.check(self._lib.sih_pdhg_get_result(self._h, index, C.byref(res)))
+        return _to_solution(res, bufs)
+
+    def time_kernels(self, reps: int = 10):
+        """Average seconds and algorithmic bytes per launch of the three step kernels
+        (elementwise primal step, A x rows step, A^T y columns step)."""
+        secs = (C.c_double * 3)()
+        byts = (C.c_double * 3)()
+        _lib.check(self._lib.sih_pdhg_time_kernels(self._h, reps, secs, byts))
+        return list(secs), list(byts)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.sih_pdhg_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
+
+
+def solve_batch(problems, config: Optional[GpuPdhgConfig] = None, **options):
+    """Solves a list of LPs in one batched launch sequence (sih_pdhg_solve_batch)."""
+    lib = _lib.load()
+    options.setdefault("algorithm", ALGO_MIXED)
+    opts = default_options(**options)
+    config = config if config is not None else GpuPdhgConfig()
+    views = [_lib.c_problem(p) for p in problems]
+    arr = (_lib.CProblem * len(views))(*[v[0] for v in views])
+    outs = [_result_buffers(p) for p in problems]
+    res_arr = (_lib.CResult * len(problems))(*[o[0] for o in outs])
+    _lib.check(lib.sih_pdhg_solve_batch(arr, len(views), C.byref(config), C.byref(opts), res_arr))
+    return [_to_solution(res_arr[i], outs[i][1]) for i in range(len(problems))]
 
 
 class GpuSolver:

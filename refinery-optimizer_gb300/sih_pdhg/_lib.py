@@ -56,7 +56,8 @@ class CResult(C.Structure):
                 ("rel_primal", C.c_double), ("rel_dual", C.c_double), ("rel_gap", C.c_double),
                 ("ref_primal", C.c_double), ("ref_dual", C.c_double), ("time_wall_sec", C.c_double),
                 ("time_solver_sec", C.c_double), ("restarts", C.c_int64), ("step_rejections", C.c_int64),
-                ("final_step", C.c_double), ("final_primal_weight", C.c_double)]
+                ("final_step", C.c_double), ("final_primal_weight", C.c_double), ("h2d_bytes", C.c_uint64),
+                ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint64)]
 
 
 _lib = None
@@ -87,8 +88,15 @@ def load() -> C.CDLL:
     lib.sih_pdhg_launch_dual_update.argtypes = [i32, vp, vp, vp, vp, vp, vp]
     lib.sih_pdhg_launch_restart.argtypes = [i32, vp, vp, vp]
     lib.sih_pdhg_launch_residuals.argtypes = [i32, i32] + [vp] * 12
-    for name in dir(lib):
-        pass
+    lib.sih_pdhg_create.argtypes = [C.POINTER(CProblem), C.c_int32, C.POINTER(GpuPdhgConfig), C.POINTER(COptions),
+                                    C.POINTER(C.c_void_p)]
+    lib.sih_pdhg_run.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.sih_pdhg_get_result.argtypes = [C.c_void_p, C.c_int32, C.POINTER(CResult)]
+    lib.sih_pdhg_time_kernels.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.sih_pdhg_destroy.argtypes = [C.c_void_p]
+    lib.sih_pdhg_destroy.restype = None
+    lib.sih_pdhg_solve_batch.argtypes = [C.POINTER(CProblem), C.c_int32, C.POINTER(GpuPdhgConfig),
+                                         C.POINTER(COptions), C.POINTER(CResult)]
     _lib = lib
     return lib
 
