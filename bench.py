@@ -80,7 +80,20 @@ def parse_args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tol", type=float, default=1e-4)
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--profile-solve", type=int, default=0, metavar="STEPS",
+                    help="profiling driver: one mixed solve of exactly STEPS steps, kernels launched one by one "
+                         "(no CUDA graph), then exit; prints no bench line")
     return ap.parse_args()
+
+
+def run_profile_solve(args) -> None:
+    """A short solve for ncu captures (run it plain first, then under ncu)."""
+    import sih_pdhg
+
+    prob = make_workload(args.workload, seed=0)
+    cfg = sih_pdhg.GpuPdhgConfig(max_iterations=args.profile_solve, tol_primal=1e-12, tol_dual=1e-12, tol_gap=1e-12)
+    sol = sih_pdhg.solve_gpu_mixed(prob, cfg, use_graph=0)
+    print(f"profile solve: {sol.simplex_iterations} steps, {sol.time_solver_sec * 1e3:.2f} ms device time")
 
 
 def dist_env():
@@ -314,7 +327,9 @@ def run_gb300(args) -> None:
 
 def main() -> None:
     args = parse_args()
-    if args.impl == "reference":
+    if args.profile_solve > 0:
+        run_profile_solve(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)
