@@ -248,6 +248,31 @@ int sih_pdhg_launch_residuals(int m, int n, const float* d_Ax, const float* d_ro
                               const float* d_l, const float* d_u, const float* d_tau, float* d_col_viols,
                               void* stream);
 
+/* ---- convergence check without allocation ---------------------------------
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory while they run (a host that hands every library a fixed device pool
+ * up front, or a loop in which the synchronising cudaMalloc / cudaFree calls
+ * are not allowed): the reference's convergence measures
+ * (core/src/gpu/gpu_solver.cpp:242-259) of a point whose data the caller
+ * already holds on the device.  Outputs d_out[0] = max row violation of A x /
+ * max_abs_b and d_out[1] = max column measure / max_abs_c (the reference's
+ * norm_p, norm_d), computed by the kernels of sih_pdhg_launch_csr_spmv,
+ * _csc_spmv and _residuals, with the working arrays in a file-scope device
+ * array of the library instead of cudaMalloc (nothing is allocated, by the
+ * library or by CUDA on its behalf).  `nnz` picks the lane groups as the
+ * launchers do.
+ * Limit: m + n <= 524,288; larger sizes return SIH_PDHG_ERR_INVALID_ARGUMENT.
+ * The array (4 MiB) stays on every GPU that loaded the library until exit.
+ * The first call on a device looks the array's address up (once per device,
+ * with that device current); make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller. */
+int sih_pdhg_check_norms_noalloc(int m, int n, int nnz, const int* d_row_ptr, const int* d_col_ind,
+                                 const float* d_csr_values, const int* d_col_ptr, const int* d_row_ind,
+                                 const float* d_csc_values, const float* d_x, const float* d_y, const float* d_c,
+                                 const float* d_l, const float* d_u, const float* d_tau, const float* d_row_l,
+                                 const float* d_row_u, float max_abs_b, float max_abs_c, float* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,6 +95,7 @@ def load() -> C.CDLL:
     lib.sih_pdhg_time_kernels.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.sih_pdhg_destroy.argtypes = [C.c_void_p]
     lib.sih_pdhg_destroy.restype = None
+    lib.sih_pdhg_check_norms_noalloc.argtypes = [i32, i32, i32] + [vp] * 14 + [C.c_float, C.c_float, vp, vp]
     lib.sih_pdhg_solve_batch.argtypes = [C.POINTER(CProblem), C.c_int32, C.POINTER(GpuPdhgConfig),
                                          C.POINTER(COptions), C.POINTER(CResult)]
     _lib = lib
