@@ -83,6 +83,8 @@ def parse_args():
     ap.add_argument("--profile-solve", type=int, default=0, metavar="STEPS",
                     help="profiling driver: one mixed solve of exactly STEPS steps, kernels launched one by one "
                          "(no CUDA graph), then exit; prints no bench line")
+    ap.add_argument("--profile-algorithm", default="mixed", choices=["mixed", "plain"],
+                    help="algorithm of --profile-solve: mixed, or plain (the reference's FP32 PDHG)")
     return ap.parse_args()
 
 
@@ -92,7 +94,8 @@ def run_profile_solve(args) -> None:
 
     prob = make_workload(args.workload, seed=0)
     cfg = sih_pdhg.GpuPdhgConfig(max_iterations=args.profile_solve, tol_primal=1e-12, tol_dual=1e-12, tol_gap=1e-12)
-    sol = sih_pdhg.solve_gpu_mixed(prob, cfg, use_graph=0)
+    algo = sih_pdhg.ALGO_MIXED if args.profile_algorithm == "mixed" else sih_pdhg.ALGO_PLAIN
+    sol = sih_pdhg.GpuSolver.solve_ex(prob, cfg, algorithm=algo, use_graph=0)
     print(f"profile solve: {sol.simplex_iterations} steps, {sol.time_solver_sec * 1e3:.2f} ms device time")
 
 

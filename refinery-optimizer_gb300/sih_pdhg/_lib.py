@@ -124,9 +124,10 @@ def _ptr(a):
 def c_problem(problem):
     """CProblem view of a sih_pdhg.Problem (keeps the arrays alive in `keep`)."""
     A = problem.A
-    keep = [np.ascontiguousarray(a) for a in (A.csc_col_ptr(), A.csc_row_ind(), A.csc_values(), A.csr_row_ptr(),
-                                              A.csr_col_ind(), A.csr_values(), problem.c, problem.col_lower,
-                                              problem.col_upper, problem.row_lower, problem.row_upper)]
+    csr = (A.csr_row_ptr(), A.csr_col_ind(), A.csr_values()) if A.has_csr() else (None, None, None)
+    keep = [None if a is None else np.ascontiguousarray(a)
+            for a in (A.csc_col_ptr(), A.csc_row_ind(), A.csc_values(), *csr, problem.c, problem.col_lower,
+                      problem.col_upper, problem.row_lower, problem.row_upper)]
     cp = CProblem(problem.num_rows(), problem.num_cols(), problem.num_nonzeros(), *[_ptr(a) for a in keep],
                   int(problem.sense), float(problem.obj_offset))
     return cp, keep

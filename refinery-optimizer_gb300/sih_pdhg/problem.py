@@ -61,13 +61,26 @@ class SparseMatrix:
             raise ValueError("csc_col_ptr must have num_cols + 1 entries")
         if self._ri.shape != self._cv.shape or self._ri.shape[0] != int(self._cp[-1]):
             raise ValueError("csc_row_ind / csc_values length must equal csc_col_ptr[-1]")
-        if csr_row_ptr is None:
-            csr_row_ptr, csr_col_ind, csr_values = csc_to_csr(self._m, self._n, self._cp, self._ri, self._cv)
-        self._rp = np.ascontiguousarray(csr_row_ptr, dtype=np.int64)
-        self._ci = np.ascontiguousarray(csr_col_ind, dtype=np.int64)
-        self._rv = np.ascontiguousarray(csr_values, dtype=np.float64)
+        self._rp = self._ci = self._rv = None
+        if csr_row_ptr is not None:
+            self._set_csr(csr_row_ptr, csr_col_ind, csr_values)
+
+    def _set_csr(self, rp, ci, rv) -> None:
+        self._rp = np.ascontiguousarray(rp, dtype=np.int64)
+        self._ci = np.ascontiguousarray(ci, dtype=np.int64)
+        self._rv = np.ascontiguousarray(rv, dtype=np.float64)
         if self._rp.shape != (self._m + 1,) or self._ci.shape[0] != self._ri.shape[0]:
             raise ValueError("CSR arrays do not match the CSC arrays")
+
+    def has_csr(self) -> bool:
+        """True once the CSR copy exists (it is built on first use; the engine
+        builds its own when a problem arrives without one)."""
+        return self._rp is not None
+
+    def _csr(self):
+        if self._rp is None:
+            self._set_csr(*csc_to_csr(self._m, self._n, self._cp, self._ri, self._cv))
+        return self._rp, self._ci, self._rv
 
     @staticmethod
     def from_triplets(m: int, n: int, rows, cols, vals, zero_tol: float = 1e-15) -> "SparseMatrix":
@@ -110,19 +123,20 @@ class SparseMatrix:
         return self._cv
 
     def csr_row_ptr(self):
-        return self._rp
+        return self._csr()[0]
 
     def csr_col_ind(self):
-        return self._ci
+        return self._csr()[1]
 
     def csr_values(self):
-        return self._rv
+        return self._csr()[2]
 
     def mat_vec(self, x) -> np.ndarray:
         """y = A x in float64 (as ``SparseMatrix::mat_vec``, sparse_matrix.cpp:90-104)."""
         x = np.asarray(x, dtype=np.float64)
-        rows = np.repeat(np.arange(self._m, dtype=np.int64), np.diff(self._rp))
-        return np.bincount(rows, weights=self._rv * x[self._ci], minlength=self._m)
+        rp, ci, rv = self._csr()
+        rows = np.repeat(np.arange(self._m, dtype=np.int64), np.diff(rp))
+        return np.bincount(rows, weights=rv * x[ci], minlength=self._m)
 
     def mat_trans_vec(self, y) -> np.ndarray:
         """z = A^T y in float64 (as ``SparseMatrix::mat_trans_vec``, sparse_matrix.cpp:115-129)."""
