@@ -98,7 +98,8 @@ typedef struct sih_pdhg_problem {
 enum {
     SIH_PDHG_ALGO_PLAIN = 0, /* the reference's FP32 PDHG: fixed diagonal steps, its termination test */
     SIH_PDHG_ALGO_MIXED = 1  /* restarted adaptive PDHG: Ruiz + Pock-Chambolle scaling, adaptive step,
-                                primal weight, KKT restarts; FP32 SpMV/updates, FP64 reductions */
+                                primal weight, KKT restarts; FP32 SpMV/updates, compensated
+                                reductions with FP64 totals */
 };
 
 /* Settings of the added entry points.  Fill with sih_pdhg_options_default(). */
@@ -124,7 +125,10 @@ typedef struct sih_pdhg_options {
     int32_t lanes_csr;         /* threads per row of the A x SpMV; 0 = automatic (autotuner or heuristic) */
     int32_t lanes_csc;         /* threads per column of the A^T y SpMV; 0 = automatic */
     int32_t heavy_factor;      /* rows/columns longer than heavy_factor * lanes go to whole warps (16) */
-    int32_t tile_nnz;          /* mixed: nonzeros per shared-memory tile of the SpMV (0 = 2048) */
+    int32_t tile_nnz;          /* mixed: nonzeros per SpMV task (0 = automatic) */
+    int32_t reorder;           /* mixed: 1 = renumber columns and rows by descending length inside each
+                                  instance so that the vector entries long segments gather share cache
+                                  lines (default); 0 = keep the input order */
 } sih_pdhg_options;
 
 /*

@@ -132,6 +132,7 @@ void sih_pdhg_options_default(sih_pdhg_options* o) {
     o->compensated = 1;
     o->dual_sign = 0;
     o->use_graph = 1;
+    o->reorder = 1;
     o->autotune = 0;
     o->verbose = 0;
     o->time_limit_sec = 0.0;

@@ -51,9 +51,14 @@ struct KktReport {
 KktReport host_kkt(const sih_pdhg_problem* p, const double* x, const double* y_pdhg, double* slack,
                    double* reduced_costs);
 
-// Runs f(begin, end) over [0, count) split across hardware threads.
+// Runs f(begin, end) over [0, count) split across hardware threads, at
+// least `min_chunk` items per thread (parallel_for: 65,536).
 template <class F>
-void parallel_for(int64_t count, F&& f);
+void parallel_for_min(int64_t count, int64_t min_chunk, F&& f);
+template <class F>
+void parallel_for(int64_t count, F&& f) {
+    parallel_for_min(count, (int64_t)1 << 16, static_cast<F&&>(f));
+}
 
 bool bound_is_finite(double v);
 int hardware_threads();
@@ -64,8 +69,8 @@ int hardware_threads();
 
 namespace sihg {
 template <class F>
-void parallel_for(int64_t count, F&& f) {
-    const int64_t min_chunk = 1 << 16;
+void parallel_for_min(int64_t count, int64_t min_chunk, F&& f) {
+    if (min_chunk < 1) min_chunk = 1;
     int t = hardware_threads();
     if (count < min_chunk * 2 || t <= 1) {
         f((int64_t)0, count);

@@ -67,8 +67,8 @@ __device__ __forceinline__ void row_dual_term(Acc& acc, float y, float rl, float
 // ---------------------------------------------------------------- step kernels
 // Elementwise part of a step.  Columns: pending float-float average update of
 // x, then x' = clip(x - tau (c + K^T y), l, u).  Rows: pending average update of y.
-__global__ void __launch_bounds__(kThreads) k_step_primal(Side cols, Side rows, Vecs V, Inst* __restrict__ st) {
-    for_each_segment_both(cols, rows, st, [&](bool is_col, const Inst& S, int r) {
+__global__ void __launch_bounds__(kThreads) k_step_primal(Chunks ch, Vecs V, Inst* __restrict__ st) {
+    for_each_element(ch, st, [&](bool is_col, const Inst& S, int r) {
         const int cur = S.cur;
         const bool avg = S.avg_pending;
         const float w = (float)S.avg_w;
@@ -112,16 +112,16 @@ struct DualStepEpi {
         const float dy = yv - p.y;
         dy2.add(dy * dy);
     }
-    __device__ void values(double (&q)[1]) {
-        q[0] = dy2.value();
+    __device__ void values(Acc (&q)[1]) {
+        q[0] = dy2;
         dy2.reset();
     }
     __device__ void finish(Inst& S, const double* tot) { S.dy2 = tot[0]; }
 };
 
-__global__ void __launch_bounds__(kThreads, 6) k_step_dual(Side rows, Vecs V, Inst* __restrict__ st) {
+__global__ void __launch_bounds__(kThreads, 4) k_step_dual(Side rows, Vecs V, Inst* __restrict__ st) {
     DualStepEpi epi{V};
-    block_engine<1, true, 1>(rows, st, epi, 0u);
+    spmv_engine<1, true, 1>(rows, st, epi, 0u);
 }
 
 // Step-size controller of one instance (PDLP adaptive step), one thread.
@@ -179,25 +179,25 @@ struct KtyStepEpi {
         inter.add(dx * (k - p.kty));
         dx2.add(dx * dx);
     }
-    __device__ void values(double (&q)[2]) {
-        q[0] = inter.value();
-        q[1] = dx2.value();
+    __device__ void values(Acc (&q)[2]) {
+        q[0] = inter;
+        q[1] = dx2;
         inter.reset();
         dx2.reset();
     }
     __device__ void finish(Inst& S, const double* tot) { step_controller(S, tot[1], tot[0]); }
 };
 
-__global__ void __launch_bounds__(kThreads, 6) k_step_kty(Side cols, Vecs V, Inst* __restrict__ st) {
+__global__ void __launch_bounds__(kThreads, 4) k_step_kty(Side cols, Vecs V, Inst* __restrict__ st) {
     KtyStepEpi epi{V};
-    block_engine<1, true, 2>(cols, st, epi, 0u);
+    spmv_engine<1, true, 2>(cols, st, epi, 0u);
 }
 
 // ---------------------------------------------------------------- evaluation kernels
 // Before an evaluation: applies a pending average update and refreshes the
 // FP32 copies x_avg, y_avg that the evaluation gathers.
-__global__ void __launch_bounds__(kThreads) k_flush_avg(Side cols, Side rows, Vecs V, Inst* __restrict__ st) {
-    for_each_segment_both(cols, rows, st, [&](bool is_col, const Inst& S, int r) {
+__global__ void __launch_bounds__(kThreads) k_flush_avg(Chunks ch, Vecs V, Inst* __restrict__ st) {
+    for_each_element(ch, st, [&](bool is_col, const Inst& S, int r) {
         const bool avg = S.avg_pending;
         const float w = (float)S.avg_w;
         if (is_col) {
@@ -241,10 +241,17 @@ struct EvalRowsEpi {
             dyl2[c].add(dy * dy);
         }
     }
-    __device__ void values(double (&q)[8]) {
-        const double v[8] = {p2[0].value(),    p2[1].value(),    (double)pinf[0], (double)pinf[1],
-                             dterm[0].value(), dterm[1].value(), dyl2[0].value(), dyl2[1].value()};
-        for (int k = 0; k < 8; ++k) q[k] = v[k];
+    __device__ void values(Acc (&q)[8]) {
+        q[0] = p2[0];
+        q[1] = p2[1];
+        q[2].s = pinf[0];
+        q[2].c = 0.f;
+        q[3].s = pinf[1];
+        q[3].c = 0.f;
+        q[4] = dterm[0];
+        q[5] = dterm[1];
+        q[6] = dyl2[0];
+        q[7] = dyl2[1];
         for (int c = 0; c < 2; ++c) {
             p2[c].reset();
             dterm[c].reset();
@@ -259,7 +266,7 @@ struct EvalRowsEpi {
 
 __global__ void __launch_bounds__(kThreads) k_eval_rows(Side rows, Vecs V, Inst* __restrict__ st) {
     EvalRowsEpi epi{V};
-    block_engine<2, true, 8>(rows, st, epi, 0x0Cu);
+    spmv_engine<2, true, 8>(rows, st, epi, 0x0Cu);
 }
 
 // Restart / termination controller of one instance after an evaluation.
@@ -377,11 +384,19 @@ struct EvalColsEpi {
             dxl2[k].add(dx * dx);
         }
     }
-    __device__ void values(double (&q)[10]) {
-        const double v[10] = {d2[0].value(),   d2[1].value(),   (double)dinf[0], (double)dinf[1],
-                              pobj[0].value(), pobj[1].value(), dterm[0].value(), dterm[1].value(),
-                              dxl2[0].value(), dxl2[1].value()};
-        for (int k = 0; k < 10; ++k) q[k] = v[k];
+    __device__ void values(Acc (&q)[10]) {
+        q[0] = d2[0];
+        q[1] = d2[1];
+        q[2].s = dinf[0];
+        q[2].c = 0.f;
+        q[3].s = dinf[1];
+        q[3].c = 0.f;
+        q[4] = pobj[0];
+        q[5] = pobj[1];
+        q[6] = dterm[0];
+        q[7] = dterm[1];
+        q[8] = dxl2[0];
+        q[9] = dxl2[1];
         for (int k = 0; k < 2; ++k) {
             d2[k].reset();
             pobj[k].reset();
@@ -400,15 +415,15 @@ struct EvalColsEpi {
 __global__ void __launch_bounds__(kThreads) k_eval_cols(Side cols, Vecs V, Inst* __restrict__ st,
                                                         unsigned* done_count) {
     EvalColsEpi epi{V, done_count};
-    block_engine<2, true, 10>(cols, st, epi, 0x0Cu);
+    spmv_engine<2, true, 10>(cols, st, epi, 0x0Cu);
 }
 
 // Applies a restart decided by the evaluation: restart to the average copies
 // the average point (and its products from the evaluation) into the current
 // buffers; either restart makes the new current point the last restart point
 // and the start of the next average.
-__global__ void __launch_bounds__(kThreads) k_restart(Side cols, Side rows, Vecs V, Inst* __restrict__ st) {
-    for_each_segment_both(cols, rows, st, [&](bool is_col, const Inst& S, int r) {
+__global__ void __launch_bounds__(kThreads) k_restart(Chunks ch, Vecs V, Inst* __restrict__ st) {
+    for_each_element(ch, st, [&](bool is_col, const Inst& S, int r) {
         const int flag = S.restart_flag;
         if (flag == 0) return;
         if (is_col) {
@@ -475,42 +490,48 @@ __global__ void k_scale_vectors(int N, int M, float* c, float* l, float* u, cons
 }
 
 // Per-instance statistics of the scaled problem for the initial step size and
-// primal weight: rows give max |a~| and |b~|^2, columns give |c~|^2.
+// primal weight: rows give max |a~| and |b~|^2, columns give |c~|^2.  Light
+// tasks cover every segment and nonzero (list tasks contribute nothing).
 template <bool ROWS>
-__device__ void init_stats_side(const Side& sd, const Vecs& V, Inst* st) {
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
-    const int rb = sd.block_run_begin[blockIdx.x], re = sd.block_run_begin[blockIdx.x + 1];
-    for (int run = rb; run < re; ++run) {
-        const Run R = sd.runs[run];
-        float amax = 0.f;
-        Acc sq;
-        for (int ti = R.task_begin + warp; ti < R.task_end; ti += nwarps) {
-            const Task t = sd.tasks[ti];
-            if (t.flags & kTaskList) continue;  // light tasks cover every segment and nonzero
-            const int k0 = sd.A.ptr[t.seg_begin], k1 = sd.A.ptr[t.seg_end];
-            for (int k = k0 + lane; k < k1; k += 32) amax = fmaxf(amax, fabsf(__int_as_float(sd.A.pairs[k].y)));
-            for (int s = t.seg_begin + lane; s < t.seg_end; s += 32) {
-                if (ROWS) {
-                    const float lo = V.rl[s], hi = V.ru[s];
-                    const float b = fin(lo) ? lo : (fin(hi) ? hi : 0.f);
-                    sq.add_prod(b, b);
-                } else {
-                    sq.add_prod(V.c[s], V.c[s]);
-                }
-            }
-        }
-        const double q[2] = {(double)amax, sq.value()};
-        double tot[2];
-        if (run_reduce<2>(sd, run, R.inst, q, 0x1u, tot) && threadIdx.x == 0) {
-            Inst& S = st[R.inst];
-            if (ROWS) {
-                S.kmax = tot[0];
-                S.b2 = tot[1];
-            } else {
-                S.c2 = tot[1];
-            }
+struct StatsEpi {
+    Vecs V;
+    float amax;
+    Acc sq;
+    __device__ void values(Acc (&q)[2]) {
+        q[0].s = amax;
+        q[0].c = 0.f;
+        q[1] = sq;
+        amax = 0.f;
+        sq.reset();
+    }
+    __device__ void finish(Inst& S, const double* tot) {
+        if (ROWS) {
+            S.kmax = tot[0];
+            S.b2 = tot[1];
+        } else {
+            S.c2 = tot[1];
         }
     }
+};
+
+template <bool ROWS>
+__device__ void init_stats_side(const Side& sd, const Vecs& V, Inst* st) {
+    const int lane = threadIdx.x & 31;
+    StatsEpi<ROWS> epi{V, 0.f, Acc{}};
+    task_loop<2>(sd, st, epi, 0x1u, [&](const Task& t, const Inst&) {
+        if (t.flags & kTaskList) return;
+        const int k0 = sd.A.ptr[t.seg_begin], k1 = sd.A.ptr[t.seg_end];
+        for (int k = k0 + lane; k < k1; k += 32) epi.amax = fmaxf(epi.amax, fabsf(__int_as_float(sd.A.pairs[k].y)));
+        for (int s = t.seg_begin + lane; s < t.seg_end; s += 32) {
+            if (ROWS) {
+                const float lo = V.rl[s], hi = V.ru[s];
+                const float b = fin(lo) ? lo : (fin(hi) ? hi : 0.f);
+                epi.sq.add_prod(b, b);
+            } else {
+                epi.sq.add_prod(V.c[s], V.c[s]);
+            }
+        }
+    });
 }
 
 __global__ void __launch_bounds__(kThreads) k_init_stats_rows(Side rows, Vecs V, Inst* __restrict__ st) {
@@ -560,14 +581,14 @@ struct StoreEpi {
     __device__ void begin(const Inst&) {}
     __device__ const float* gather(int) const { return vec; }
     __device__ void apply(int i, const SegDot<1>& d, const Pre&) { out[i] = d.s[0]; }
-    __device__ void values(double (&q)[1]) { q[0] = 0.0; }
+    __device__ void values(Acc (&q)[1]) { q[0].reset(); }
     __device__ void finish(Inst&, const double*) {}
 };
 
 __global__ void __launch_bounds__(kThreads) k_spmv_store(Side side, Inst* __restrict__ st, const float* __restrict__ vec,
                                                          float* __restrict__ out) {
     StoreEpi epi{vec, out};
-    block_engine<1, false, 1>(side, st, epi, 0u);
+    spmv_engine<1, false, 1>(side, st, epi, 0u);
 }
 
 // ---------------------------------------------------------------- host: schedule
@@ -577,8 +598,7 @@ static int pow2_floor(int v) {
     return p;
 }
 
-void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, int blocks,
-                   SideSchedule& out) {
+void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out) {
     const int B = (int)inst_off.size() - 1;
     out = SideSchedule{};
     out.light_max.assign(B, 0);
@@ -632,39 +652,21 @@ void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off
             if (L == 32) break;
         }
     }
-    // contiguous, work-balanced task ranges per block, cut into per-instance runs
+    // reduction groups: at most kGroup consecutive tasks of one instance
     const int nt = (int)out.tasks.size();
-    std::vector<double> pre(nt + 1, 0.0);
-    for (int t = 0; t < nt; ++t) {
-        const Task& k = out.tasks[t];
-        double w = 64.0;
-        if (k.flags & kTaskList) {
-            for (int h = k.seg_begin; h < k.seg_end; ++h)
-                w += 16.0 + (ptr[out.list_idx[h] + 1] - ptr[out.list_idx[h]]);
-        } else {
-            w += (ptr[k.seg_end] - ptr[k.seg_begin]) + 8.0 * (k.seg_end - k.seg_begin);
-        }
-        pre[t + 1] = pre[t] + w;
-    }
-    blocks = std::max(1, blocks);
-    out.block_run_begin.assign(blocks + 1, 0);
+    out.task_group.assign(nt, 0);
+    out.inst_group_begin.assign(B + 1, 0);
     int t = 0;
-    for (int g = 0; g < blocks; ++g) {
-        out.block_run_begin[g] = (int)out.runs.size();
-        int te = t;
-        const double target = pre[nt] * (g + 1) / blocks;
-        while (te < nt && (g == blocks - 1 || pre[te + 1] <= target)) ++te;
-        while (t < te) {
-            int e = t;
-            while (e < te && out.tasks[e].inst == out.tasks[t].inst) ++e;
-            out.runs.push_back(Run{out.tasks[t].inst, t, e, 0});
-            t = e;
+    for (int b = 0; b < B; ++b) {
+        out.inst_group_begin[b] = (int)out.group_begin.size();
+        while (t < nt && out.tasks[t].inst == b) {
+            const int g = (int)out.group_begin.size();
+            out.group_begin.push_back(t);
+            for (int k = 0; k < kGroup && t < nt && out.tasks[t].inst == b; ++k, ++t) out.task_group[t] = g;
         }
     }
-    out.block_run_begin[blocks] = (int)out.runs.size();
-    out.inst_run_begin.assign(B + 1, (int)out.runs.size());
-    for (int r = (int)out.runs.size() - 1; r >= 0; --r) out.inst_run_begin[out.runs[r].inst] = r;
-    for (int b = B - 1; b >= 0; --b) out.inst_run_begin[b] = std::min(out.inst_run_begin[b], out.inst_run_begin[b + 1]);
+    out.inst_group_begin[B] = (int)out.group_begin.size();
+    out.group_begin.push_back(nt);
 }
 
 // ---------------------------------------------------------------- host: solver
@@ -674,6 +676,21 @@ MixedSolver::~MixedSolver() {
     if (ev_start_) cudaEventDestroy(ev_start_);
     if (ev_stop_) cudaEventDestroy(ev_stop_);
     if (stream_) cudaStreamDestroy(stream_);
+}
+
+// Stable order of `cnt` segments by descending length (counting sort); the
+// identity without `reorder`.
+static void order_by_length(const int* ptr, int cnt, bool reorder, int* perm) {
+    if (!reorder || cnt <= 1) {
+        for (int k = 0; k < cnt; ++k) perm[k] = k;
+        return;
+    }
+    int maxlen = 0;
+    for (int k = 0; k < cnt; ++k) maxlen = std::max(maxlen, ptr[k + 1] - ptr[k]);
+    std::vector<int> start((size_t)maxlen + 2, 0);
+    for (int k = 0; k < cnt; ++k) start[maxlen - (ptr[k + 1] - ptr[k]) + 1]++;
+    for (int v = 0; v <= maxlen; ++v) start[v + 1] += start[v];
+    for (int k = 0; k < cnt; ++k) perm[start[maxlen - (ptr[k + 1] - ptr[k])]++] = k;
 }
 
 static int upload(DevMem& d, const void* h, size_t bytes, cudaStream_t s) {
@@ -713,62 +730,114 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     std::vector<int> csr_ptr((size_t)M_ + 1), csc_ptr((size_t)N_ + 1);
     std::vector<Pair> csr((size_t)nnz), csc((size_t)nnz);
     std::vector<float> c(N_), l(N_), u(N_), rl(M_), ru(M_);
-    {
-        std::vector<long long> k_off(B_ + 1, 0);
-        for (int b = 0; b < B_; ++b) k_off[b + 1] = k_off[b] + probs[b]->nnz;
-        parallel_for(B_, [&](int64_t b0, int64_t b1) {
-            for (int64_t b = b0; b < b1; ++b) {
-                const HostProblem& p = *probs[b];
-                const int ro = row_off_[b], co = col_off_[b];
-                const long long ko = k_off[b];
-                for (int i = 0; i < p.m; ++i) csr_ptr[ro + i] = (int)(p.csr_ptr[i] + ko);
-                for (int j = 0; j < p.n; ++j) csc_ptr[co + j] = (int)(p.csc_ptr[j] + ko);
-                for (int k = 0; k < p.nnz; ++k) {
-                    csr[ko + k] = Pair{p.csr[k].idx + co, p.csr[k].val};
-                    csc[ko + k] = Pair{p.csc[k].idx + ro, p.csc[k].val};
+    // Renumbering inside each instance (opts.reorder): columns and rows by
+    // descending length.  The entries that long segments share then sit in
+    // few cache lines of the gathered vectors (for Zipf-like column lengths
+    // most of A x's gathers hit an L1-sized prefix of x).  perm: new -> old,
+    // inv: old -> new, both local to the instance.
+    col_perm_.assign(N_, 0);
+    row_perm_.assign(M_, 0);
+    std::vector<int> col_inv(N_), row_inv(M_);
+    std::vector<long long> k_off(B_ + 1, 0);
+    for (int b = 0; b < B_; ++b) k_off[b + 1] = k_off[b] + probs[b]->nnz;
+    const bool reorder = opts.reorder != 0;
+    parallel_for_min(2 * (int64_t)B_, 1, [&](int64_t w0, int64_t w1) {
+        for (int64_t w = w0; w < w1; ++w) {
+            const int b = (int)(w >> 1);
+            const HostProblem& p = *probs[b];
+            const bool cols = (w & 1) == 0;
+            const std::vector<int>& ptr = cols ? p.csc_ptr : p.csr_ptr;
+            const int cnt = cols ? p.n : p.m;
+            const int off = cols ? col_off_[b] : row_off_[b];
+            int* perm = (cols ? col_perm_.data() : row_perm_.data()) + off;
+            int* inv = (cols ? col_inv.data() : row_inv.data()) + off;
+            order_by_length(ptr.data(), cnt, reorder, perm);
+            for (int k = 0; k < cnt; ++k) inv[perm[k]] = k;
+            // pointers of the renumbered segments
+            int* dst = (cols ? csc_ptr.data() : csr_ptr.data()) + off;
+            long long acc = k_off[b];
+            for (int k = 0; k < cnt; ++k) {
+                dst[k] = (int)acc;
+                acc += ptr[perm[k] + 1] - ptr[perm[k]];
+            }
+        }
+    });
+    csr_ptr[M_] = (int)nnz;
+    csc_ptr[N_] = (int)nnz;
+    // entries and vectors, in pieces of at most 32k segments
+    struct Piece {
+        int b, cols, k0, k1;
+    };
+    std::vector<Piece> pieces;
+    for (int b = 0; b < B_; ++b)
+        for (int side = 0; side < 2; ++side) {
+            const int cnt = side == 0 ? probs[b]->n : probs[b]->m;
+            for (int k0 = 0; k0 < cnt; k0 += 32768) pieces.push_back(Piece{b, side == 0, k0, std::min(cnt, k0 + 32768)});
+        }
+    // infinite bounds are +-inf (|v| >= 1e20 counts as infinite)
+    auto inf_clean = [](double v) -> float {
+        if (std::isinf(v) || std::fabs(v) >= 1e20) return v > 0 ? INFINITY : -INFINITY;
+        return (float)v;
+    };
+    parallel_for_min((int64_t)pieces.size(), 1, [&](int64_t q0, int64_t q1) {
+        for (int64_t q = q0; q < q1; ++q) {
+            const Piece& pc = pieces[q];
+            const HostProblem& p = *probs[pc.b];
+            const int ro = row_off_[pc.b], co = col_off_[pc.b];
+            if (pc.cols) {
+                for (int jn = pc.k0; jn < pc.k1; ++jn) {
+                    const int j = col_perm_[co + jn];
+                    int at = csc_ptr[co + jn];
+                    for (int k = p.csc_ptr[j]; k < p.csc_ptr[j + 1]; ++k, ++at)
+                        csc[at] = Pair{row_inv[ro + p.csc[k].idx] + ro, p.csc[k].val};
+                    c[co + jn] = p.c[j];
+                    l[co + jn] = inf_clean(p.src->col_lower[j]);
+                    u[co + jn] = inf_clean(p.src->col_upper[j]);
                 }
-                // infinite bounds are +-inf (|v| >= 1e20 counts as infinite)
-                auto inf_clean = [](double v) -> float {
-                    if (std::isinf(v) || std::fabs(v) >= 1e20) return v > 0 ? INFINITY : -INFINITY;
-                    return (float)v;
-                };
-                for (int j = 0; j < p.n; ++j) {
-                    c[co + j] = p.c[j];
-                    l[co + j] = inf_clean(p.src->col_lower[j]);
-                    u[co + j] = inf_clean(p.src->col_upper[j]);
-                }
-                for (int i = 0; i < p.m; ++i) {
-                    rl[ro + i] = inf_clean(p.src->row_lower[i]);
-                    ru[ro + i] = inf_clean(p.src->row_upper[i]);
+            } else {
+                for (int in = pc.k0; in < pc.k1; ++in) {
+                    const int i = row_perm_[ro + in];
+                    int at = csr_ptr[ro + in];
+                    for (int k = p.csr_ptr[i]; k < p.csr_ptr[i + 1]; ++k, ++at)
+                        csr[at] = Pair{col_inv[co + p.csr[k].idx] + co, p.csr[k].val};
+                    rl[ro + in] = inf_clean(p.src->row_lower[i]);
+                    ru[ro + in] = inf_clean(p.src->row_upper[i]);
                 }
             }
-        });
-        csr_ptr[M_] = (int)nnz;
-        csc_ptr[N_] = (int)nnz;
-    }
-    // ---- schedules (tasks, block ranges, runs)
+        }
+    });
+    // ---- schedules (tasks and reduction groups per side, element chunks)
     int occ = 0;
     SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_step_dual, kThreads, 0));
     grid_ = std::max(1, sm_count_ * std::max(1, occ));
-    // default task size: about four tasks per resident warp, within [128, 2048]
+    int occ_e = 0;
+    SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, k_step_primal, kThreads, 0));
+    elem_grid_ = std::max(1, sm_count_ * std::max(1, occ_e));
+    // default task size: about three tasks per resident warp, within [128, 2048]
     const long long warps = (long long)grid_ * (kThreads / 32);
     task_nnz_ = opts.tile_nnz > 0 ? opts.tile_nnz
-                                  : (int)std::max(128LL, std::min(2048LL, nnz / std::max(1LL, 4 * warps)));
+                                  : (int)std::max(128LL, std::min(2048LL, nnz / std::max(1LL, 3 * warps)));
     task_nnz_ = std::max(32, std::min(1 << 20, task_nnz_));
     SideSchedule rs, cs;
-    make_schedule(csr_ptr, row_off_, task_nnz_, grid_, rs);
-    make_schedule(csc_ptr, col_off_, task_nnz_, grid_, cs);
+    make_schedule(csr_ptr, row_off_, task_nnz_, rs);
+    make_schedule(csc_ptr, col_off_, task_nnz_, cs);
 
     SIHG_TRY(upload(csr_ptr_, csr_ptr.data(), sizeof(int) * csr_ptr.size(), s));
     SIHG_TRY(upload(csc_ptr_, csc_ptr.data(), sizeof(int) * csc_ptr.size(), s));
     SIHG_TRY(upload(csr_pairs_, csr.data(), sizeof(Pair) * csr.size(), s));
     SIHG_TRY(upload(csc_pairs_, csc.data(), sizeof(Pair) * csc.size(), s));
+    // per side: tickets [B] + counters [2] + group tickets [ngroups], zeroed once;
+    // the kernels leave them zero
+    const size_t ng_r = rs.group_begin.size() - 1, ng_c = cs.group_begin.size() - 1;
+    const size_t nticket = 2 * ((size_t)B_ + 2) + ng_r + ng_c;
+    SIHG_TRY(tickets_.alloc(sizeof(unsigned) * nticket));
+    SIHG_CUDA(cudaMemsetAsync(tickets_.as<void>(), 0, sizeof(unsigned) * nticket, s));
     auto upload_schedule = [&](const SideSchedule& sc, DevMem& mem, const SegMatrix& A, DevMem& part,
-                               unsigned* tickets, Side& side) -> int {
-        const size_t nt = sc.tasks.size(), nr = sc.runs.size();
-        const size_t bytes = sizeof(Task) * nt + sizeof(Run) * nr +
-                             sizeof(int) * (sc.block_run_begin.size() + sc.inst_run_begin.size() +
-                                            sc.list_idx.size() + sc.light_max.size()) + 64;
+                               unsigned* tick, Side& side) -> int {
+        const size_t nt = sc.tasks.size(), ng = sc.group_begin.size() - 1;
+        const size_t bytes = sizeof(Task) * nt +
+                             sizeof(int) * (sc.list_idx.size() + sc.light_max.size() + sc.task_group.size() +
+                                            sc.group_begin.size() + sc.inst_group_begin.size()) + 96;
         std::vector<char> buf(bytes, 0);
         size_t off = 0;
         auto put = [&](const void* src, size_t n) {
@@ -778,25 +847,47 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
             return at;
         };
         const size_t o_t = put(sc.tasks.data(), sizeof(Task) * nt);
-        const size_t o_r = put(sc.runs.data(), sizeof(Run) * nr);
-        const size_t o_b = put(sc.block_run_begin.data(), sizeof(int) * sc.block_run_begin.size());
-        const size_t o_i = put(sc.inst_run_begin.data(), sizeof(int) * sc.inst_run_begin.size());
         const size_t o_h = put(sc.list_idx.data(), sizeof(int) * sc.list_idx.size());
         const size_t o_x = put(sc.light_max.data(), sizeof(int) * sc.light_max.size());
+        const size_t o_g = put(sc.task_group.data(), sizeof(int) * sc.task_group.size());
+        const size_t o_b = put(sc.group_begin.data(), sizeof(int) * sc.group_begin.size());
+        const size_t o_i = put(sc.inst_group_begin.data(), sizeof(int) * sc.inst_group_begin.size());
         buf.resize(std::max<size_t>(off, 16));
         SIHG_TRY(upload(mem, buf.data(), buf.size(), s));
-        SIHG_TRY(part.alloc(sizeof(double) * kQ * std::max<size_t>(1, nr)));
+        SIHG_TRY(part.alloc(sizeof(float2) * kQ * (std::max<size_t>(1, nt) + std::max<size_t>(1, ng))));
         char* d = mem.as<char>();
-        side = Side{A, (const Task*)(d + o_t), (int)nt, (const Run*)(d + o_r), (const int*)(d + o_b),
-                    (const int*)(d + o_i), (const int*)(d + o_h), (const int*)(d + o_x), part.as<double>(), tickets};
+        float2* tp = part.as<float2>();
+        side = Side{A,
+                    (const Task*)(d + o_t),
+                    (int)nt,
+                    (const int*)(d + o_h),
+                    (const int*)(d + o_x),
+                    (const int*)(d + o_g),
+                    (const int*)(d + o_b),
+                    (const int*)(d + o_i),
+                    tp,
+                    tp + (size_t)kQ * std::max<size_t>(1, nt),
+                    tick + B_ + 2,  // group tickets
+                    tick,           // instance tickets
+                    tick + B_};     // counters
         return SIH_PDHG_OK;
     };
-    SIHG_TRY(tickets_.alloc(sizeof(unsigned) * 2 * (B_ + 1)));
-    SIHG_CUDA(cudaMemsetAsync(tickets_.as<void>(), 0, sizeof(unsigned) * 2 * (B_ + 1), s));
-    SIHG_TRY(upload_schedule(rs, row_sched_, SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()}, row_part_,
-                             tickets_.as<unsigned>(), rows_));
+    unsigned* tk = tickets_.as<unsigned>();
+    SIHG_TRY(upload_schedule(rs, row_sched_, SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()}, row_part_, tk,
+                             rows_));
     SIHG_TRY(upload_schedule(cs, col_sched_, SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, col_part_,
-                             tickets_.as<unsigned>() + (B_ + 1), cols_));
+                             tk + B_ + 2 + ng_r, cols_));
+    {
+        std::vector<int4> ch;
+        for (int side = 0; side < 2; ++side) {
+            const std::vector<int>& off = side == 0 ? col_off_ : row_off_;
+            for (int b = 0; b < B_; ++b)
+                for (int e0 = off[b]; e0 < off[b + 1]; e0 += kChunk)
+                    ch.push_back(make_int4(e0, std::min(off[b + 1], e0 + kChunk), b, side == 0 ? 1 : 0));
+        }
+        SIHG_TRY(upload(chunks_, ch.data(), sizeof(int4) * std::max<size_t>(1, ch.size()), s));
+        chunks_all_ = Chunks{chunks_.as<int4>(), (int)ch.size()};
+    }
 
     // ---- vectors: 11 column vectors, 10 row vectors (layout of Vecs) + float-float averages
     SIHG_TRY(colvec_.alloc(sizeof(float) * (size_t)N_ * 11));
@@ -874,7 +965,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
 int MixedSolver::launch_step(cudaStream_t s) {
     launches_ += 3;
     Inst* st = state_.as<Inst>();
-    k_step_primal<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
+    k_step_primal<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st);
     k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
     k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
     SIHG_LAUNCH_CHECK();
@@ -884,10 +975,10 @@ int MixedSolver::launch_step(cudaStream_t s) {
 int MixedSolver::launch_eval(cudaStream_t s) {
     launches_ += 4;
     Inst* st = state_.as<Inst>();
-    k_flush_avg<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
+    k_flush_avg<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st);
     k_eval_rows<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
     k_eval_cols<<<grid_, kThreads, 0, s>>>(cols_, V_, st, done_count_.as<unsigned>());
-    k_restart<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
+    k_restart<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st);
     SIHG_LAUNCH_CHECK();
     return SIH_PDHG_OK;
 }
@@ -962,7 +1053,9 @@ int MixedSolver::run() {
         cudaError_t e = cudaEventCreateWithFlags(&ev[w], cudaEventDisableTiming);
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate", __FILE__, __LINE__);
     }
-    const long long max_blocks = (cfg_.max_iterations + eval_freq_ - 1) / eval_freq_ + 1;
+    // the evaluation that ends block k sees attempts = (k + 1) * eval_freq and
+    // stops every instance at the iteration limit, so this many blocks suffice
+    const long long max_blocks = std::max<long long>(1, (cfg_.max_iterations + eval_freq_ - 1) / eval_freq_);
     timed_out_ = false;
     if (rc == SIH_PDHG_OK) {
         cudaEventRecord(ev_start_, s);
@@ -1016,8 +1109,8 @@ int MixedSolver::fetch(int b, std::vector<double>& x, std::vector<double>& y) {
     SIHG_CUDA(cudaMemcpy(dr.data(), V_.drow + ro, sizeof(float) * m, cudaMemcpyDeviceToHost));
     x.resize(n);
     y.resize(m);
-    for (int j = 0; j < n; ++j) x[j] = (double)xs[j] * (double)dc[j];
-    for (int i = 0; i < m; ++i) y[i] = (double)ys[i] * (double)dr[i];
+    for (int j = 0; j < n; ++j) x[col_perm_[co + j]] = (double)xs[j] * (double)dc[j];
+    for (int i = 0; i < m; ++i) y[row_perm_[ro + i]] = (double)ys[i] * (double)dr[i];
     return SIH_PDHG_OK;
 }
 
@@ -1032,7 +1125,7 @@ int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
     for (int k = 0; k < 3 && rc == SIH_PDHG_OK; ++k) {
         cudaEventRecord(e0, s);
         for (int i = 0; i < reps; ++i) {
-            if (k == 0) k_step_primal<<<grid_, kThreads, 0, s>>>(cols_, rows_, V_, st);
+            if (k == 0) k_step_primal<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st);
             if (k == 1) k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
             if (k == 2) k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
         }

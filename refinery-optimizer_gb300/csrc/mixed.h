@@ -1,4 +1,5 @@
-// Mixed-precision restarted adaptive PDHG (scaled, FP32 SpMV, FP64 reductions)
+// Mixed-precision restarted adaptive PDHG (scaled, FP32 SpMV, compensated
+// reductions with FP64 instance totals)
 // for one LP or a batch of LPs; see mixed.cu for the algorithm.
 #pragma once
 
@@ -10,8 +11,10 @@
 
 namespace sihg {
 
-constexpr int kQ = 12;         // partial slots per task
+constexpr int kQ = 12;         // reduction slots per task / group
 constexpr int kThreads = 256;  // threads per block of every task kernel
+constexpr int kGroup = 32;     // tasks per reduction group (one per lane of the reducing warp)
+constexpr int kChunk = 2048;   // elements per chunk of the elementwise passes
 
 // Unit of SpMV work of one instance (see warp.cuh): a LIGHT task is the
 // contiguous segment range [seg_begin, seg_end) (longer segments skipped); a
@@ -27,15 +30,7 @@ constexpr int kTaskList = 1;
 __host__ __device__ inline int task_lanes(int flags) { return (flags >> 8) & 0xff; }
 constexpr int kTaskSegs = 1024;  // max segments per light task
 
-// The tasks of one instance inside one block's task range.
-struct Run {
-    int inst;
-    int task_begin;
-    int task_end;
-    int pad;
-};
-
-// Per-instance device state (all reductions and controller scalars in FP64).
+// Per-instance device state (reduction totals and controller scalars in FP64).
 struct Inst {
     // control
     int done;          // 0 running, 1 converged, 2 iteration limit, 3 numerical failure
@@ -66,27 +61,34 @@ struct Side {
     SegMatrix A;
     const Task* tasks;
     int ntasks;
-    const Run* runs;
-    const int* block_run_begin;  // [grid + 1]
-    const int* inst_run_begin;   // [B + 1]
-    const int* list_idx;         // segment ids of the list tasks
-    const int* light_max;        // [B] longest segment a light task processes
-    double* partials;            // [nruns * kQ]
-    unsigned* tickets;           // [B]
+    const int* list_idx;          // segment ids of the list tasks
+    const int* light_max;         // [B] longest segment a light task processes
+    const int* task_group;        // [ntasks] reduction group of each task
+    const int* group_begin;       // [ngroups + 1] first task of each group
+    const int* inst_group_begin;  // [B + 1] first group of each instance
+    float2* task_part;            // [ntasks * kQ] task partials (float-float)
+    float2* group_part;           // [ngroups * kQ] group partials
+    unsigned* group_tickets;      // [ngroups]
+    unsigned* tickets;            // [B] completed groups per instance
+    unsigned* counters;           // [2] next dynamic task, warps that left
+};
+
+// Chunks of the elementwise passes: {begin, end, instance, is_col}, columns
+// first; a chunk never crosses an instance.
+struct Chunks {
+    const int4* chunks;
+    int n;
 };
 
 // Host-side schedule of one side.
 struct SideSchedule {
     std::vector<Task> tasks;
-    std::vector<Run> runs;
-    std::vector<int> block_run_begin, inst_run_begin, list_idx, light_max;
+    std::vector<int> list_idx, light_max, task_group, group_begin, inst_group_begin;
 };
 
 // Host: tasks of every instance of one side (light tasks of at most task_nnz
-// light nonzeros, then list tasks per length class), cut into `blocks`
-// contiguous work-balanced ranges and per-instance runs.
-void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, int blocks,
-                   SideSchedule& out);
+// light nonzeros, then list tasks per length class) and their reduction groups.
+void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out);
 
 struct Vecs {
     // column side (length N)
@@ -147,9 +149,12 @@ class MixedSolver {
     cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;
     cudaGraphExec_t graphs_[1] = {nullptr};
     std::vector<int> row_off_, col_off_;
+    std::vector<int> col_perm_, row_perm_;  // device order -> instance-local original index
     DevMem csr_ptr_, csc_ptr_, csr_pairs_, csc_pairs_, row_sched_, col_sched_;
-    DevMem row_part_, col_part_, tickets_, colvec_, rowvec_, state_, done_count_, accvec_;
+    DevMem row_part_, col_part_, tickets_, colvec_, rowvec_, state_, done_count_, accvec_, chunks_;
     Side rows_{}, cols_{};
+    Chunks chunks_all_{};
+    int elem_grid_ = 1;
     Vecs V_{};
     std::vector<Inst> host_inst_;
 };

@@ -8,25 +8,33 @@
 //     instance and one length class, so that the lane groups of a warp get
 //     segments within a factor 2 of each other (Zipf-like columns stay
 //     balanced); its lane-group width grows with the class.
-// Tasks are ordered by instance.  Each block owns a contiguous, nonzero-balanced
-// range of tasks, cut into RUNS (the block's tasks of one instance).  The
-// warps of the block share a run's tasks; every lane keeps FP32 compensated
-// accumulators (Acc).  After a run the block reduces them once (FP64 only at
-// this step) into the run's slot and takes a ticket of the instance; the block
-// completing the instance reduces the instance's run slots in order
-// (deterministic) and runs its controller.
+// Tasks are ordered by instance and cut into GROUPS of at most kGroup tasks of
+// one instance.
+//
+// Scheduling: every warp of the grid is a worker.  Warp w starts on task w and
+// then takes the next task from a counter of the side (one atomic per task),
+// so the work spreads over the SMs as it runs instead of by a static split.
+// Reductions stay deterministic: a task's lanes reduce their compensated
+// accumulators (Acc) in a fixed butterfly into the task's slot; the warp that
+// completes a group (ticket) reduces the group's task slots in task order; the
+// warp that completes an instance reduces its group slots in group order,
+// converts the totals to FP64 and runs the instance's controller.  No warp
+// ever waits for another.
 //
 // Inside a task, groups of L lanes walk the segments; each lane issues kBatch
-// pair loads, then kBatch gathers, then the FMAs; the next segment's pointers
-// and the epilogue operands (Epi::pre) are loaded before the current dot.
+// pair loads, then kBatch gathers, then the FMAs.  The loads are software
+// pipelined: the first pairs of the next segment (and the next batch inside a
+// long segment) are in flight while the current batch gathers; pointers run
+// two segments ahead; the epilogue operands (Epi::pre) load before the dot.
 //
 // Epilogue interface (Epi):
 //   using Pre;  Pre pre(int seg) const          operands of a segment (global loads)
-//   void begin(const Inst&)                    per-run setup (vectors to gather)
+//   void begin(const Inst&)                    per-task setup (vectors to gather)
 //   const float* gather(int v) const           vector gathered by the nonzero indices
 //   void apply(int seg, const SegDot<NV>&, const Pre&)
-//   template <int Q> values(double (&q)[Q])    this thread's partial reductions; reset them
-//   void finish(Inst&, const double* total)    instance controller (one thread)
+//   void values(Acc (&q)[Q])                   this lane's partial reductions; resets them
+//                                              (a max travels in q.s with q.c = 0)
+//   void finish(Inst&, const double* total)    instance controller (one lane)
 #pragma once
 
 #include "mixed.h"
@@ -42,18 +50,64 @@ struct SegDot {
     __device__ __forceinline__ float f(int v) const { return __fadd_rn(s[v], e[v]); }
 };
 
+// Loads one batch of a lane's pairs (entries k, k + L, ..., k + (kBatch-1) L
+// below `end`); the rest are zero.
+__device__ __forceinline__ void load_batch(bool on, const int2* __restrict__ pairs, int k, int end, int L,
+                                           int2 (&p)[kBatch]) {
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) p[u] = (on && k + u * L < end) ? ld_pair(pairs + k + u * L) : make_int2(0, 0);
+}
+
+// Dot products of one segment with the NV gathered vectors, this lane's share
+// (entries beg+sub, +L, ...), reduced over the lane group.  `p` holds the
+// lane's first batch of pairs on entry (loaded ahead by the caller); inside a
+// long segment the next batch's pairs load while the current batch gathers.
+// Plain: kBatch FMA chains per vector, summed pairwise (as seg_dot);
+// COMP: Dot2 (two-product + two-sum) per vector.
 template <int NV, bool COMP, class Epi>
-__device__ __forceinline__ void seg_group_dot(const SegMatrix& A, int beg, int end, int sub, int L, bool active,
-                                              Epi& epi, SegDot<NV>& d) {
+__device__ __forceinline__ void seg_dots(const int2* __restrict__ pairs, int beg, int end, int sub, int L,
+                                         bool active, Epi& epi, int2 (&p)[kBatch], SegDot<NV>& d) {
+    float acc[NV][kBatch], s2[NV], e2[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-        float s = 0.f, e = 0.f;
-        if (active) {
-            if (COMP)
-                seg_dot2(A.pairs, beg, end, sub, L, epi.gather(v), s, e);
-            else
-                s = seg_dot(A.pairs, beg, end, sub, L, epi.gather(v));
+        s2[v] = e2[v] = 0.f;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) acc[v][u] = 0.f;
+    }
+    if (active) {
+        for (int k = beg + sub;; k += kBatch * L) {
+            const int kn = k + kBatch * L;
+            const bool more = kn < end;
+            int2 q[kBatch];
+            load_batch(more, pairs, kn, end, L, q);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const float* __restrict__ vec = epi.gather(v);
+                float g[kBatch];
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) g[u] = (k + u * L < end) ? ld_vec(vec + p[u].x) : 0.f;
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                    if (COMP) {
+                        float pr, pe, ss, se;
+                        two_prod(__int_as_float(p[u].y), g[u], pr, pe);
+                        two_sum(s2[v], pr, ss, se);
+                        s2[v] = ss;
+                        e2[v] = __fadd_rn(e2[v], __fadd_rn(pe, se));
+                    } else {
+                        acc[v][u] = fmaf(__int_as_float(p[u].y), g[u], acc[v][u]);
+                    }
+                }
+            }
+            if (!more) break;
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) p[u] = q[u];
         }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        float s = COMP ? s2[v] : (acc[v][0] + acc[v][1]) + (acc[v][2] + acc[v][3]);
+        float e = e2[v];
         if (COMP)
             group_sum2(s, e, L);
         else
@@ -65,36 +119,55 @@ __device__ __forceinline__ void seg_group_dot(const SegMatrix& A, int beg, int e
 
 // One task on one warp: groups of L lanes walk its segments (a light task's
 // contiguous range, skipping segments longer than light_max, or a list task's
-// listed segments).
+// listed segments).  Software pipeline over segments: the pointers of the
+// segment two ahead and the first pairs of the next segment are in flight
+// while the current segment gathers.
 template <int NV, bool COMP, bool LIST, class Epi>
 __device__ __forceinline__ void run_task(const SegMatrix& A, const int* __restrict__ list, const Task& t,
                                          int light_max, Epi& epi) {
+    static_assert(kBatch == 4, "seg_dots sums four FMA chains");
     const int L = task_lanes(t.flags);
     const int lane = threadIdx.x & 31, sub = lane & (L - 1), gpw = 32 / L;
     int k = t.seg_begin + lane / L;
-    int r = -1, beg = 0, end = 0;
+    int r0 = -1, b0 = 0, e0 = 0, r1 = -1, b1 = 0, e1 = 0;
     if (k < t.seg_end) {
-        r = LIST ? list[k] : k;
-        beg = A.ptr[r];
-        end = A.ptr[r + 1];
+        r0 = LIST ? list[k] : k;
+        b0 = A.ptr[r0];
+        e0 = A.ptr[r0 + 1];
     }
+    if (k + gpw < t.seg_end) {
+        r1 = LIST ? list[k + gpw] : k + gpw;
+        b1 = A.ptr[r1];
+        e1 = A.ptr[r1 + 1];
+    }
+    bool act0 = k < t.seg_end && (LIST || e0 - b0 <= light_max);
+    int2 p0[kBatch];
+    load_batch(act0, A.pairs, b0 + sub, e0, L, p0);
     for (int wb = t.seg_begin; wb < t.seg_end; wb += gpw, k += gpw) {
-        const int kn = k + gpw;
-        int rn = -1, nbeg = 0, nend = 0;
-        if (kn < t.seg_end) {  // next segment's pointers in flight during this one
-            rn = LIST ? list[kn] : kn;
-            nbeg = A.ptr[rn];
-            nend = A.ptr[rn + 1];
+        const int k2 = k + 2 * gpw;
+        int r2 = -1, b2 = 0, e2 = 0;
+        if (k2 < t.seg_end) {
+            r2 = LIST ? list[k2] : k2;
+            b2 = A.ptr[r2];
+            e2 = A.ptr[r2 + 1];
         }
-        const bool active = k < t.seg_end && (LIST || end - beg <= light_max);
+        const bool act1 = k + gpw < t.seg_end && (LIST || e1 - b1 <= light_max);
+        int2 p1[kBatch];
+        load_batch(act1, A.pairs, b1 + sub, e1, L, p1);
         typename Epi::Pre pre{};
-        if (active && sub == 0) pre = epi.pre(r);
+        if (act0 && sub == 0) pre = epi.pre(r0);
         SegDot<NV> d;
-        seg_group_dot<NV, COMP>(A, beg, end, sub, L, active, epi, d);
-        if (active && sub == 0) epi.apply(r, d, pre);
-        r = rn;
-        beg = nbeg;
-        end = nend;
+        seg_dots<NV, COMP>(A.pairs, b0, e0, sub, L, act0, epi, p0, d);
+        if (act0 && sub == 0) epi.apply(r0, d, pre);
+        r0 = r1;
+        b0 = b1;
+        e0 = e1;
+        act0 = act1;
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) p0[u] = p1[u];
+        r1 = r2;
+        b1 = b2;
+        e1 = e2;
     }
 }
 
@@ -106,114 +179,173 @@ __device__ __forceinline__ void run_any_task(const Side& side, const Task& t, in
         run_task<NV, COMP, false>(side.A, side.list_idx, t, light_max, epi);
 }
 
-// Reduction of one run (all threads of the block): block-reduces Q values
-// (sum, or max for the bits of max_mask) into the run's slot and takes a ticket
-// of the instance.  Returns true (in every thread) on the block that completed
-// the instance; `total` (thread 0) then holds the instance totals, reduced
-// over its run slots in order.
+// ---------------------------------------------------------------- deterministic reductions
+// (s1 + c1) + (s2 + c2) with the rounding error of the leading sum kept; the
+// result does not depend on the order of the operands.
+__device__ __forceinline__ Acc acc_plus(const Acc& a, const Acc& b) {
+    Acc r;
+    float e;
+    two_sum(a.s, b.s, r.s, e);
+    r.c = __fadd_rn(__fadd_rn(a.c, b.c), e);
+    return r;
+}
+
+__device__ __forceinline__ Acc acc_join(const Acc& a, const Acc& b, bool is_max) {
+    if (is_max) {
+        Acc r;
+        r.s = fmaxf(a.s, b.s);
+        r.c = 0.f;
+        return r;
+    }
+    return acc_plus(a, b);
+}
+
+// Butterfly over the warp: every lane ends with the same value.
 template <int Q>
-__device__ bool run_reduce(const Side& side, int run, int inst, const double (&q)[Q], unsigned max_mask,
-                           double (&total)[Q]) {
-    __shared__ double red[Q][32];
-    __shared__ bool s_last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+__device__ __forceinline__ void warp_reduce_acc(Acc (&q)[Q], unsigned max_mask) {
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         const bool is_max = (max_mask >> i) & 1u;
-        const double v = is_max ? warp_maxd(q[i]) : warp_sum(q[i]);
-        if (lane == 0) red[i][warp] = v;
-    }
-    __syncthreads();
-    if (warp == 0) {
 #pragma unroll
-        for (int i = 0; i < Q; ++i) {
-            const bool is_max = (max_mask >> i) & 1u;
-            double v = lane < nwarps ? red[i][lane] : 0.0;
-            v = is_max ? warp_maxd(v) : warp_sum(v);
-            if (lane == 0) side.partials[(size_t)run * kQ + i] = v;
+        for (int o = 16; o > 0; o >>= 1) {
+            Acc b;
+            b.s = __shfl_xor_sync(FULL_MASK, q[i].s, o);
+            b.c = __shfl_xor_sync(FULL_MASK, q[i].c, o);
+            q[i] = acc_join(q[i], b, is_max);
         }
-        if (lane == 0) {
-            __threadfence();
-            const unsigned ib = side.inst_run_begin[inst], ie = side.inst_run_begin[inst + 1];
-            const unsigned old = atomicAdd(&side.tickets[inst], 1u);
-            s_last = old + 1u == ie - ib;
-        }
-    }
-    __syncthreads();
-    const bool last = s_last;
-    if (last) {
-        __threadfence();
-        const int ib = side.inst_run_begin[inst], ie = side.inst_run_begin[inst + 1];
-#pragma unroll
-        for (int i = 0; i < Q; ++i) {
-            const bool is_max = (max_mask >> i) & 1u;
-            double acc = 0.0;
-            for (int k = ib + (int)threadIdx.x; k < ie; k += blockDim.x) {
-                const double v = __ldcg(&side.partials[(size_t)k * kQ + i]);
-                acc = is_max ? fmax(acc, v) : acc + v;
-            }
-            acc = is_max ? warp_maxd(acc) : warp_sum(acc);
-            if (lane == 0) red[i][warp] = acc;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                const bool is_max = (max_mask >> i) & 1u;
-                double acc = 0.0;
-                for (int w = 0; w < nwarps; ++w) acc = is_max ? fmax(acc, red[i][w]) : acc + red[i][w];
-                total[i] = acc;
-            }
-            side.tickets[inst] = 0u;
-        }
-    }
-    __syncthreads();
-    return last;
-}
-
-// Runs the block's runs.  With ALLOW_COMP the tasks of an instance with
-// `refine` set run compensated (Dot2).  Q = reduced values, max_mask marks the
-// ones reduced by max instead of sum.
-template <int NV, bool ALLOW_COMP, int Q, class Epi>
-__device__ void block_engine(const Side& side, Inst* st, Epi& epi, unsigned max_mask) {
-    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int rb = side.block_run_begin[blockIdx.x], re = side.block_run_begin[blockIdx.x + 1];
-    for (int run = rb; run < re; ++run) {
-        const Run R = side.runs[run];
-        Inst& S = st[R.inst];
-        if (S.done) continue;  // uniform: the flag only changes after the instance's last run
-        epi.begin(S);
-        const bool comp = ALLOW_COMP && S.refine;
-        const int lmax = side.light_max[R.inst];
-        for (int ti = R.task_begin + warp; ti < R.task_end; ti += nwarps) {
-            const Task t = side.tasks[ti];
-            if (comp)
-                run_any_task<NV, true>(side, t, lmax, epi);
-            else
-                run_any_task<NV, false>(side, t, lmax, epi);
-        }
-        double q[Q], tot[Q];
-        epi.values(q);
-        if (run_reduce<Q>(side, run, R.inst, q, max_mask, tot) && threadIdx.x == 0) epi.finish(S, tot);
-        __syncthreads();
     }
 }
 
-// Elementwise pass: warp-strided over the light tasks of both sides (columns
-// first; light tasks cover every segment), lane-strided over their segments.
-template <class F>
-__device__ __forceinline__ void for_each_segment_both(const Side& cols, const Side& rows, Inst* st, F&& f) {
-    const int wpb = blockDim.x >> 5;
-    const int gw = blockIdx.x * wpb + (threadIdx.x >> 5), nw = gridDim.x * wpb;
+template <int Q>
+__device__ __forceinline__ void store_slot(float2* slot, const Acc (&q)[Q]) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) slot[i] = make_float2(q[i].s, q[i].c);
+}
+
+// Ticket increment with release (the caller's earlier slot stores become
+// visible before it) and acquire (the last arriver sees every other caller's
+// slots): atom.acq_rel at GPU scope, no separate fence.
+__device__ __forceinline__ unsigned ticket_add(unsigned* t) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(t) : "memory");
+    return old;
+}
+
+template <int Q>
+__device__ __forceinline__ void load_slot_join(const float2* slot, Acc (&q)[Q], unsigned max_mask) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const float2 v = __ldcg(slot + i);
+        Acc b;
+        b.s = v.x;
+        b.c = v.y;
+        q[i] = acc_join(q[i], b, (max_mask >> i) & 1u);
+    }
+}
+
+// After a task of instance t.inst has left its lane partials in q (all lanes):
+// writes the task slot and runs the group / instance completion.  Returns
+// true (in every lane) on the warp that completed the instance; `total` then
+// holds the instance's FP64 totals.
+template <int Q>
+__device__ bool task_complete(const Side& side, int ti, int inst, Acc (&q)[Q], unsigned max_mask,
+                              double (&total)[Q]) {
     const int lane = threadIdx.x & 31;
-    for (int ti = gw; ti < cols.ntasks + rows.ntasks; ti += nw) {
-        const bool is_col = ti < cols.ntasks;
-        const Side& sd = is_col ? cols : rows;
-        const Task t = sd.tasks[is_col ? ti : ti - cols.ntasks];
-        if (t.flags & kTaskList) continue;
-        const Inst& S = st[t.inst];
+    warp_reduce_acc<Q>(q, max_mask);
+    const int g = side.task_group[ti];
+    const int gb = side.group_begin[g], ge = side.group_begin[g + 1];
+    unsigned last = 0;
+    if (lane == 0) {
+        store_slot<Q>(side.task_part + (size_t)ti * kQ, q);
+        last = ticket_add(&side.group_tickets[g]) + 1u == (unsigned)(ge - gb);
+    }
+    last = __shfl_sync(FULL_MASK, last, 0);
+    __syncwarp();  // orders lane 0's acquire before the other lanes' slot loads
+    if (!last) return false;
+    // this warp completed group g: reduce its task slots in task order
+    Acc v[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) v[i].reset();
+    if (gb + lane < ge) load_slot_join<Q>(side.task_part + (size_t)(gb + lane) * kQ, v, max_mask);
+    warp_reduce_acc<Q>(v, max_mask);
+    unsigned ilast = 0;
+    if (lane == 0) {
+        side.group_tickets[g] = 0u;
+        store_slot<Q>(side.group_part + (size_t)g * kQ, v);
+        const int ngr = side.inst_group_begin[inst + 1] - side.inst_group_begin[inst];
+        ilast = ticket_add(&side.tickets[inst]) + 1u == (unsigned)ngr;
+    }
+    ilast = __shfl_sync(FULL_MASK, ilast, 0);
+    __syncwarp();
+    if (!ilast) return false;
+    // this warp completed the instance: reduce its group slots (lane k takes
+    // groups k, k + 32, ... in order, then the butterfly)
+    const int ib = side.inst_group_begin[inst], ie = side.inst_group_begin[inst + 1];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) v[i].reset();
+    for (int k = ib + lane; k < ie; k += 32) load_slot_join<Q>(side.group_part + (size_t)k * kQ, v, max_mask);
+    warp_reduce_acc<Q>(v, max_mask);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) total[i] = (double)v[i].s + (double)v[i].c;
+    if (lane == 0) side.tickets[inst] = 0u;
+    return true;
+}
+
+// Worker loop of one warp over the side's tasks.  `body(t, S)` does the work
+// of one task (all lanes), leaving partials in `epi`.
+template <int Q, class Epi, class Body>
+__device__ __forceinline__ void task_loop(const Side& side, Inst* st, Epi& epi, unsigned max_mask, Body&& body) {
+    const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    int ti = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    while (ti < side.ntasks) {
+        // the next task index is fetched while this task runs
+        int next = 0;
+        if (lane == 0) next = (int)atomicAdd(&side.counters[0], 1u) + nw;
+        const Task t = side.tasks[ti];
+        Inst& S = st[t.inst];
+        if (!S.done) {  // uniform over the warp; it only changes after the instance's last task
+            body(t, S);
+            Acc q[Q];
+            epi.values(q);
+            double tot[Q];
+            if (task_complete<Q>(side, ti, t.inst, q, max_mask, tot) && lane == 0) epi.finish(S, tot);
+            __syncwarp();
+        }
+        ti = __shfl_sync(FULL_MASK, next, 0);
+    }
+    // the last warp to leave resets the counters for the next launch
+    if (lane == 0 && atomicAdd(&side.counters[1], 1u) + 1u == (unsigned)nw) {
+        side.counters[0] = 0u;
+        side.counters[1] = 0u;
+    }
+}
+
+// SpMV engine: the tasks of the side with the epilogue Epi.  With ALLOW_COMP
+// the tasks of an instance with `refine` set run compensated (Dot2).
+template <int NV, bool ALLOW_COMP, int Q, class Epi>
+__device__ __forceinline__ void spmv_engine(const Side& side, Inst* st, Epi& epi, unsigned max_mask) {
+    task_loop<Q>(side, st, epi, max_mask, [&](const Task& t, const Inst& S) {
+        epi.begin(S);
+        const int lmax = side.light_max[t.inst];
+        if (ALLOW_COMP && S.refine)
+            run_any_task<NV, true>(side, t, lmax, epi);
+        else
+            run_any_task<NV, false>(side, t, lmax, epi);
+    });
+}
+
+// Elementwise pass over every column (is_col) and row of the running
+// instances: blocks take chunks of kChunk consecutive elements of one
+// instance, threads stride through a chunk (coalesced).
+template <class F>
+__device__ __forceinline__ void for_each_element(const Chunks& ch, Inst* st, F&& f) {
+    for (int c = blockIdx.x; c < ch.n; c += gridDim.x) {
+        const int4 d = ch.chunks[c];  // begin, end, instance, is_col
+        const Inst& S = st[d.z];
         if (S.done) continue;
-        for (int r = t.seg_begin + lane; r < t.seg_end; r += 32) f(is_col, S, r);
+        const bool is_col = d.w != 0;
+        for (int r = d.x + threadIdx.x; r < d.y; r += blockDim.x) f(is_col, S, r);
     }
 }
 
