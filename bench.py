@@ -12,9 +12,16 @@ entry point with host buffers (conversion, upload, scaling, solve, download and
 FP64 KKT packing inside the timed region).
 
 Workloads (seeded synthetic LPs, FP64 data, generators in sih_pdhg.generators):
-  zipf-500kx1m  m=500,000 (half equalities), n=1,000,000, 12M nonzeros, column
-                counts Zipf(1.5) clipped to [2, 2000] and rescaled (default)
-  random-2kx5k  m=2,000, n=5,000, 8 nonzeros per column
+  zipf-500kx1m   m=500,000 (half equalities), n=1,000,000, 12M nonzeros, column
+                 counts Zipf(1.5) clipped to [2, 2000] and rescaled (default)
+  random-2kx5k   m=2,000, n=5,000, 8 nonzeros per column
+  refinery-168p  one block-angular refinery planning LP of 168 hourly periods
+                 (m=149,856, n=237,552, 1.1M nonzeros)
+  refinery-512   512 price-shock / outage scenarios of that LP with 24..336
+                 periods, solved as one batch (every instance to the tolerance);
+                 the line adds the sequential plain-algorithm solves of the same
+                 scenarios on the same GPU (sampled) for the batched-vs-plain ratio
+  refinery-64    the first 64 of those scenarios (a shorter batch)
 
 Multi-GPU: replicas (each rank solves its own copy; scaling "weak").
 --impl reference times the reference's algorithm (plain FP32 PDHG) through its
@@ -25,6 +32,7 @@ the same tolerance on the same LP.
 from __future__ import annotations
 
 import argparse
+import itertools
 import json
 import os
 import statistics
@@ -53,6 +61,9 @@ PLAIN_ITERS_TO_TOL = {
 PLAIN_ITERS_LOWER_BOUND = {
     "zipf-500kx1m": 200000,
     "random-2kx5k": 20000,
+    "refinery-168p": 100000,
+    "refinery-512": 100000,
+    "refinery-64": 100000,
 }
 
 # DRAM bytes per launch of the dominant kernel, read from one ncu capture of
@@ -61,14 +72,28 @@ PLAIN_ITERS_LOWER_BOUND = {
 NCU_TRAFFIC_PER_LAUNCH = {}
 
 
+WORKLOADS = ["zipf-500kx1m", "random-2kx5k", "refinery-168p", "refinery-512", "refinery-64"]
+
+
 def make_workload(name: str, seed: int = 0):
-    from sih_pdhg.generators import small_random_lp, zipf_lp
+    """The workload's LP, or its list of LPs for a batch workload."""
+    from sih_pdhg.generators import refinery_lp, refinery_scenarios, small_random_lp, zipf_lp
 
     if name == "zipf-500kx1m":
         return zipf_lp(500_000, 1_000_000, 12_000_000, seed)
     if name == "random-2kx5k":
         return small_random_lp(2000, 5000, 8, seed)
+    if name == "refinery-168p":
+        return refinery_lp(168, seed)
+    if name == "refinery-512":
+        return list(refinery_scenarios(512, seed))
+    if name == "refinery-64":
+        return list(itertools.islice(refinery_scenarios(512, seed), 64))
     raise SystemExit(f"unknown workload {name}")
+
+
+def as_list(w):
+    return w if isinstance(w, list) else [w]
 
 
 def parse_args():
@@ -76,10 +101,12 @@ def parse_args():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="zipf-500kx1m", choices=["zipf-500kx1m", "random-2kx5k"])
+    ap.add_argument("--workload", default="zipf-500kx1m", choices=WORKLOADS)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tol", type=float, default=1e-4)
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--plain-sample", type=int, default=4,
+                    help="batch workloads: scenarios timed with the plain algorithm for the sequential estimate")
     ap.add_argument("--profile-solve", type=int, default=0, metavar="STEPS",
                     help="profiling driver: one mixed solve of exactly STEPS steps, kernels launched one by one "
                          "(no CUDA graph), then exit; prints no bench line")
@@ -196,7 +223,9 @@ def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    prob = make_workload(args.workload)
+    work = make_workload(args.workload)
+    probs = as_list(work)
+    prob = probs[0]
     threads = os.cpu_count() or 1
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
@@ -207,6 +236,8 @@ def run_reference(args) -> None:
     lower = its_needed is None
     if lower:
         its_needed = PLAIN_ITERS_LOWER_BOUND[args.workload]
+    # a batch is timed on its first scenario and scaled by nonzeros
+    nnz_scale = sum(p.num_nonzeros() for p in probs) / prob.num_nonzeros()
     # each step: a bounded sample of iterations sized to ~2 s
     probe = cpu_plain_per_iteration(data, 3, threads)
     sample = max(3, int(2.0 / max(probe, 1e-6)))
@@ -214,16 +245,19 @@ def run_reference(args) -> None:
         cpu_plain_per_iteration(data, max(3, sample // 4), threads)
     ests = []
     for _ in range(args.steps):
-        ests.append(cpu_plain_per_iteration(data, sample, threads) * its_needed)
+        ests.append(cpu_plain_per_iteration(data, sample, threads) * its_needed * nnz_scale)
     value = statistics.mean(ests)
     note = (f"{sample} iterations of the reference algorithm's CPU port per step, x {its_needed} iterations "
             + ("(lower bound: the plain algorithm did not reach the tolerance within this many)" if lower else
                "needed to reach the tolerance"))
+    if len(probs) > 1:
+        note += f"; timed on scenario 0, x {nnz_scale:.1f} by nonzeros for all {len(probs)} scenarios"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, seed 0)",
-            "config": {"workload": args.workload, "m": prob.num_rows(), "n": prob.num_cols(),
-                       "nnz": prob.num_nonzeros(), "tol": args.tol, "algorithm": "plain FP32 PDHG (reference)"},
+            "config": {"workload": args.workload, "m": sum(p.num_rows() for p in probs),
+                       "n": sum(p.num_cols() for p in probs), "nnz": sum(p.num_nonzeros() for p in probs),
+                       "tol": args.tol, "algorithm": "plain FP32 PDHG (reference)"},
             "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": note},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -261,10 +295,12 @@ def run_gb300(args) -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    prob = make_workload(args.workload, seed=0)
+    work = make_workload(args.workload, seed=0)
+    probs = as_list(work)
+    batch = isinstance(work, list)
     tol = args.tol
     cfg = sih_pdhg.GpuPdhgConfig(max_iterations=1_000_000, tol_primal=tol, tol_dual=tol, tol_gap=tol)
-    handle = sih_pdhg.PdhgHandle(prob, cfg, algorithm=sih_pdhg.ALGO_MIXED)
+    handle = sih_pdhg.PdhgHandle(probs, cfg, algorithm=sih_pdhg.ALGO_MIXED)
     for _ in range(args.warmup):
         handle.run()
     barrier()
@@ -276,9 +312,10 @@ def run_gb300(args) -> None:
     barrier()
     wall = time.perf_counter() - t_wall
     clock_info = clocks.stop()
-    sol = handle.result(0)
+    sols = [handle.result(i) for i in range(len(probs))]
     step = max_over_ranks(statistics.mean(times))
-    launches = sol.kernel_launches * args.steps
+    launches = sols[0].kernel_launches * args.steps
+    iters = [s.simplex_iterations for s in sols]
 
     # roofline of the dominant SpMV kernel (live CUDA-event timing on the solver stream)
     secs, byts = handle.time_kernels(20)
@@ -291,32 +328,41 @@ def run_gb300(args) -> None:
 
     # end to end through the C ABI with host buffers (upload .. download inside)
     e2e_times = []
-    e2e_sol = None
-    for i in range(2):
+    e2e_sols = None
+    for i in range(1 if batch else 2):
         barrier()
         t0 = time.perf_counter()
-        e2e_sol = sih_pdhg.solve_gpu_mixed(prob, cfg)
+        e2e_sols = sih_pdhg.solve_batch(probs, cfg) if batch else [sih_pdhg.solve_gpu_mixed(probs[0], cfg)]
         torch.cuda.synchronize()
-        if i > 0 or args.steps <= 1:
+        if batch or i > 0 or args.steps <= 1:
             e2e_times.append(time.perf_counter() - t0)
     e2e = max_over_ranks(statistics.mean(e2e_times))
+    h2d = sum(int(s.h2d_bytes) for s in e2e_sols)  # per instance: matrix, vectors
+    d2h = sum(int(s.d2h_bytes) for s in e2e_sols)
 
     if rank != 0:
         return
-    m, n, nnz = prob.num_rows(), prob.num_cols(), prob.num_nonzeros()
+    m = sum(p.num_rows() for p in probs)
+    n = sum(p.num_cols() for p in probs)
+    nnz = sum(p.num_nonzeros() for p in probs)
     plain_its = PLAIN_ITERS_TO_TOL.get(args.workload)
+    cfg_desc = {"workload": args.workload, "m": m, "n": n, "nnz": nnz, "tol": tol,
+                "algorithm": "mixed-precision restarted adaptive PDHG", "parallelism": f"replicas x{world}",
+                "l2": "working set larger than the 129 MB L2 (no flush needed)" if nnz * 16 > 129e6
+                else "working set L2-resident (small LP: latency-bound)"}
+    if batch:
+        cfg_desc["instances"] = len(probs)
     line = {
         "metric": METRIC, "value": step, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded generator, seed 0)",
-        "config": {"workload": args.workload, "m": m, "n": n, "nnz": nnz, "tol": tol,
-                   "algorithm": "mixed-precision restarted adaptive PDHG", "parallelism": f"replicas x{world}",
-                   "l2": "working set ~300 MB > 129 MB L2 (no flush needed)"},
-        "iterations": sol.simplex_iterations, "restarts": sol.restarts, "status": int(sol.status),
-        "rel_kkt": [sol.rel_primal, sol.rel_dual, sol.rel_gap], "wall_s_per_step": wall / args.steps,
+        "config": cfg_desc,
+        "iterations": max(iters), "restarts": sols[0].restarts,
+        "status": max(int(s.status) for s in sols),
+        "rel_kkt": [max(s.rel_primal for s in sols), max(s.rel_dual for s in sols), max(s.rel_gap for s in sols)],
+        "wall_s_per_step": wall / args.steps,
         "clocks": clock_info,
-        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(e2e_sol.h2d_bytes),
-                "d2h_bytes_per_step": int(e2e_sol.d2h_bytes)},
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_src,
@@ -324,8 +370,49 @@ def run_gb300(args) -> None:
                      "algorithmic_bytes_per_launch": byts[dom], "all_kernels_gbs": all_gbs},
         "plain_reference_iterations_to_tol": plain_its,
     }
-    line["cpu_baseline"] = cpu_pdlp_sample(prob, sol.simplex_iterations, args.cpu_sample_seconds)
+    if batch:
+        line["iterations_per_instance"] = {"min": min(iters), "median": int(statistics.median(iters)),
+                                           "max": max(iters)}
+        line["plain_gpu_sequential"] = plain_sequential_sample(probs, tol, args.plain_sample)
+    # CPU baseline: the FP64 port of the same algorithm on one instance, scaled
+    # to the whole job by nonzero-steps
+    big = max(range(len(probs)), key=lambda i: probs[i].num_nonzeros()) if not batch else 0
+    cb = cpu_pdlp_sample(probs[big], iters[big], args.cpu_sample_seconds)
+    if batch:
+        work_all = sum(it * p.num_nonzeros() for it, p in zip(iters, probs))
+        scale = work_all / (iters[big] * probs[big].num_nonzeros())
+        cb["value"] *= scale
+        cb["sample"] += (f"; x {scale:.1f} to cover all {len(probs)} instances "
+                         f"(sum over instances of steps x nonzeros)")
+    line["cpu_baseline"] = cb
     print(json.dumps(line), flush=True)
+
+
+def plain_sequential_sample(probs, tol: float, count: int) -> dict:
+    """The reference algorithm (plain FP32 PDHG) on the same GPU, one scenario
+    after another: `count` scenarios (evenly spaced through the batch) solved
+    with an iteration cap; the estimate for all scenarios scales the sampled
+    seconds by the batch's nonzeros.  Scenarios that stop at the cap make the
+    estimate a lower bound."""
+    import sih_pdhg
+
+    cap = 100_000
+    pick = sorted(set(int(round(k)) for k in [i * (len(probs) - 1) / max(1, count - 1) for i in range(count)]))
+    secs, nnz_s, reached = 0.0, 0, 0
+    for i in pick:
+        p = probs[i]
+        cfg = sih_pdhg.GpuPdhgConfig(max_iterations=cap, tol_primal=tol, tol_dual=tol, tol_gap=tol)
+        sol = sih_pdhg.solve_gpu_pdhg(p, cfg)
+        secs += sol.time_solver_sec
+        nnz_s += p.num_nonzeros()
+        if max(sol.rel_primal, sol.rel_dual, sol.rel_gap) <= tol:
+            reached += 1
+    total_nnz = sum(p.num_nonzeros() for p in probs)
+    est = secs * total_nnz / max(1, nnz_s)
+    return {"value": est, "unit": "s", "lower_bound": reached < len(pick),
+            "sample": f"{len(pick)} scenarios solved one after another with the plain algorithm "
+                      f"(iteration cap {cap}); {reached} reached relative KKT <= {tol:g}; "
+                      f"{secs:.2f} s device time scaled by nonzeros to all {len(probs)} scenarios"}
 
 
 def main() -> None:

@@ -591,6 +591,80 @@ __global__ void __launch_bounds__(kThreads) k_spmv_store(Side side, Inst* __rest
     spmv_engine<1, false, 1>(side, st, epi, 0u);
 }
 
+// ---------------------------------------------------------------- active lists
+// After an evaluation: the tasks (both sides) and element chunks of the
+// instances still running, in instance order.  One block computes the
+// per-instance offsets (prefix sums over the instances) ...
+__global__ void k_compact_offsets(int B, const Inst* __restrict__ st, const int* __restrict__ rt,
+                                  const int* __restrict__ ct, const int* __restrict__ hb, int* off, int* counts,
+                                  unsigned* row_counter, unsigned* col_counter) {
+    __shared__ int carry[3];
+    __shared__ int wsum[3][32];
+    if (threadIdx.x < 3) carry[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {  // task counters restart with the new lists
+        *row_counter = 0u;
+        *col_counter = 0u;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int base = 0; base < B; base += blockDim.x) {
+        const int b = base + threadIdx.x;
+        int v[3] = {0, 0, 0};
+        if (b < B && !st[b].done) {
+            v[0] = rt[b + 1] - rt[b];
+            v[1] = ct[b + 1] - ct[b];
+            v[2] = hb[b + 1] - hb[b];
+        }
+        int incl[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            int x = v[k];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL_MASK, x, o);
+                if (lane >= o) x += y;
+            }
+            incl[k] = x;
+            if (lane == 31) wsum[k][warp] = x;
+        }
+        __syncthreads();
+        if (b < B) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                int before = carry[k];
+                for (int w = 0; w < warp; ++w) before += wsum[k][w];
+                off[k * B + b] = before + incl[k] - v[k];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            int t = 0;
+            for (int w = 0; w < nwarps; ++w) t += wsum[threadIdx.x][w];
+            carry[threadIdx.x] += t;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) counts[threadIdx.x] = carry[threadIdx.x];
+}
+
+// ... and the grid scatters the entries of the running instances.
+__global__ void k_compact_fill(int B, const Inst* __restrict__ st, Side rows, Side cols, Chunks ch,
+                               const int* __restrict__ off) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows.ntasks; i += stride) {
+        const int b = rows.tasks[i].inst;
+        if (!st[b].done) rows.active[off[b] + i - rows.inst_task_begin[b]] = i;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cols.ntasks; i += stride) {
+        const int b = cols.tasks[i].inst;
+        if (!st[b].done) cols.active[off[B + b] + i - cols.inst_task_begin[b]] = i;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ch.n; i += stride) {
+        const int b = ch.chunks[i].z;
+        if (!st[b].done) ch.active[off[2 * B + b] + i - ch.inst_begin[b]] = i;
+    }
+}
+
 // ---------------------------------------------------------------- host: schedule
 static int pow2_floor(int v) {
     int p = 1;
@@ -667,6 +741,9 @@ void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off
     }
     out.inst_group_begin[B] = (int)out.group_begin.size();
     out.group_begin.push_back(nt);
+    out.inst_task_begin.assign(B + 1, nt);
+    for (int k = nt - 1; k >= 0; --k) out.inst_task_begin[out.tasks[k].inst] = k;
+    for (int b = B - 1; b >= 0; --b) out.inst_task_begin[b] = std::min(out.inst_task_begin[b], out.inst_task_begin[b + 1]);
 }
 
 // ---------------------------------------------------------------- host: solver
@@ -837,7 +914,8 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
         const size_t nt = sc.tasks.size(), ng = sc.group_begin.size() - 1;
         const size_t bytes = sizeof(Task) * nt +
                              sizeof(int) * (sc.list_idx.size() + sc.light_max.size() + sc.task_group.size() +
-                                            sc.group_begin.size() + sc.inst_group_begin.size()) + 96;
+                                            sc.group_begin.size() + sc.inst_group_begin.size() +
+                                            sc.inst_task_begin.size()) + 112;
         std::vector<char> buf(bytes, 0);
         size_t off = 0;
         auto put = [&](const void* src, size_t n) {
@@ -852,6 +930,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
         const size_t o_g = put(sc.task_group.data(), sizeof(int) * sc.task_group.size());
         const size_t o_b = put(sc.group_begin.data(), sizeof(int) * sc.group_begin.size());
         const size_t o_i = put(sc.inst_group_begin.data(), sizeof(int) * sc.inst_group_begin.size());
+        const size_t o_s = put(sc.inst_task_begin.data(), sizeof(int) * sc.inst_task_begin.size());
         buf.resize(std::max<size_t>(off, 16));
         SIHG_TRY(upload(mem, buf.data(), buf.size(), s));
         SIHG_TRY(part.alloc(sizeof(float2) * kQ * (std::max<size_t>(1, nt) + std::max<size_t>(1, ng))));
@@ -869,7 +948,10 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
                     tp + (size_t)kQ * std::max<size_t>(1, nt),
                     tick + B_ + 2,  // group tickets
                     tick,           // instance tickets
-                    tick + B_};     // counters
+                    tick + B_,      // counters
+                    (const int*)(d + o_s),
+                    nullptr,
+                    nullptr};
         return SIH_PDHG_OK;
     };
     unsigned* tk = tickets_.as<unsigned>();
@@ -879,14 +961,34 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
                              tk + B_ + 2 + ng_r, cols_));
     {
         std::vector<int4> ch;
-        for (int side = 0; side < 2; ++side) {
-            const std::vector<int>& off = side == 0 ? col_off_ : row_off_;
-            for (int b = 0; b < B_; ++b)
+        std::vector<int> ch_begin(B_ + 1, 0);
+        for (int b = 0; b < B_; ++b) {
+            ch_begin[b] = (int)ch.size();
+            for (int side = 0; side < 2; ++side) {
+                const std::vector<int>& off = side == 0 ? col_off_ : row_off_;
                 for (int e0 = off[b]; e0 < off[b + 1]; e0 += kChunk)
                     ch.push_back(make_int4(e0, std::min(off[b + 1], e0 + kChunk), b, side == 0 ? 1 : 0));
+            }
         }
-        SIHG_TRY(upload(chunks_, ch.data(), sizeof(int4) * std::max<size_t>(1, ch.size()), s));
-        chunks_all_ = Chunks{chunks_.as<int4>(), (int)ch.size()};
+        ch_begin[B_] = (int)ch.size();
+        const size_t nch = ch.size();
+        // chunk descriptors, then the chunk instance index
+        std::vector<char> buf(sizeof(int4) * std::max<size_t>(1, nch) + sizeof(int) * (B_ + 1), 0);
+        std::memcpy(buf.data(), ch.data(), sizeof(int4) * nch);
+        std::memcpy(buf.data() + sizeof(int4) * std::max<size_t>(1, nch), ch_begin.data(), sizeof(int) * (B_ + 1));
+        SIHG_TRY(upload(chunks_, buf.data(), buf.size(), s));
+        // active lists: rows tasks, cols tasks, chunks; 3 counts; 3 x B offsets
+        const size_t nr = rows_.ntasks, nc = cols_.ntasks;
+        SIHG_TRY(active_.alloc(sizeof(int) * (nr + nc + nch + 3 + 3 * (size_t)B_ + 8)));
+        int* a = active_.as<int>();
+        rows_.active = a;
+        cols_.active = a + nr;
+        int* cnt = a + nr + nc + nch;
+        rows_.nactive = cnt;
+        cols_.nactive = cnt + 1;
+        chunks_all_ = Chunks{chunks_.as<int4>(), (int)nch,
+                             (const int*)(chunks_.as<char>() + sizeof(int4) * std::max<size_t>(1, nch)),
+                             a + nr + nc, cnt + 2};
     }
 
     // ---- vectors: 11 column vectors, 10 row vectors (layout of Vecs) + float-float averages
@@ -980,6 +1082,18 @@ int MixedSolver::launch_eval(cudaStream_t s) {
     k_eval_cols<<<grid_, kThreads, 0, s>>>(cols_, V_, st, done_count_.as<unsigned>());
     k_restart<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st);
     SIHG_LAUNCH_CHECK();
+    return launch_compact(s);
+}
+
+int MixedSolver::launch_compact(cudaStream_t s) {
+    launches_ += 2;
+    Inst* st = state_.as<Inst>();
+    int* off = rows_.nactive + 3;  // 3 x B offsets after the three counts
+    k_compact_offsets<<<1, 1024, 0, s>>>(B_, st, rows_.inst_task_begin, cols_.inst_task_begin,
+                                         chunks_all_.inst_begin, off, rows_.nactive, rows_.counters,
+                                         cols_.counters);
+    k_compact_fill<<<elem_grid_, kThreads, 0, s>>>(B_, st, rows_, cols_, chunks_all_, off);
+    SIHG_LAUNCH_CHECK();
     return SIH_PDHG_OK;
 }
 
@@ -1002,6 +1116,7 @@ int MixedSolver::reset_state() {
     SIHG_CUDA(cudaMemcpyAsync(state_.as<Inst>(), host_inst_.data(), sizeof(Inst) * B_, cudaMemcpyHostToDevice, s));
     SIHG_CUDA(cudaMemsetAsync(done_count_.as<void>(), 0, sizeof(unsigned), s));
     launches_ += 5;
+    SIHG_TRY(launch_compact(s));  // every instance runs: full task and chunk lists
     // initial point x = clip(0, l~, u~), y = 0; averages and last points equal it
     k_init_point<<<g, 256, 0, s>>>(N_, M_, V_);
     SIHG_LAUNCH_CHECK();
@@ -1074,7 +1189,7 @@ int MixedSolver::run() {
             if (opts_.use_graph) {
                 cudaError_t e = cudaGraphLaunch(graphs_[0], s);
                 if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
-                launches_ += 3ull * eval_freq_ + 4ull;
+                launches_ += 3ull * eval_freq_ + 6ull;
             } else {
                 for (int k = 0; k < eval_freq_ && rc == SIH_PDHG_OK; ++k) rc = launch_step(s);
                 if (rc == SIH_PDHG_OK) rc = launch_eval(s);

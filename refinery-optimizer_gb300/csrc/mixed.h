@@ -70,20 +70,26 @@ struct Side {
     float2* group_part;           // [ngroups * kQ] group partials
     unsigned* group_tickets;      // [ngroups]
     unsigned* tickets;            // [B] completed groups per instance
-    unsigned* counters;           // [2] next dynamic task, warps that left
+    unsigned* counters;           // [2] dynamic task counter (zeroed by each compaction), spare
+    const int* inst_task_begin;   // [B + 1] first task of each instance
+    int* active;                  // [ntasks] tasks of the running instances (rebuilt after evaluations)
+    int* nactive;                 // [1] entries of `active`
 };
 
-// Chunks of the elementwise passes: {begin, end, instance, is_col}, columns
-// first; a chunk never crosses an instance.
+// Chunks of the elementwise passes: {begin, end, instance, is_col}, grouped
+// by instance; a chunk never crosses an instance.
 struct Chunks {
     const int4* chunks;
     int n;
+    const int* inst_begin;  // [B + 1] first chunk of each instance
+    int* active;            // [n] chunks of the running instances
+    int* nactive;           // [1]
 };
 
 // Host-side schedule of one side.
 struct SideSchedule {
     std::vector<Task> tasks;
-    std::vector<int> list_idx, light_max, task_group, group_begin, inst_group_begin;
+    std::vector<int> list_idx, light_max, task_group, group_begin, inst_group_begin, inst_task_begin;
 };
 
 // Host: tasks of every instance of one side (light tasks of at most task_nnz
@@ -131,6 +137,7 @@ class MixedSolver {
 
   private:
     int reset_state();
+    int launch_compact(cudaStream_t s);
     int record_graph();
 
     std::vector<const HostProblem*> probs_;
@@ -151,7 +158,7 @@ class MixedSolver {
     std::vector<int> row_off_, col_off_;
     std::vector<int> col_perm_, row_perm_;  // device order -> instance-local original index
     DevMem csr_ptr_, csc_ptr_, csr_pairs_, csc_pairs_, row_sched_, col_sched_;
-    DevMem row_part_, col_part_, tickets_, colvec_, rowvec_, state_, done_count_, accvec_, chunks_;
+    DevMem row_part_, col_part_, tickets_, colvec_, rowvec_, state_, done_count_, accvec_, chunks_, active_;
     Side rows_{}, cols_{};
     Chunks chunks_all_{};
     int elem_grid_ = 1;

@@ -11,9 +11,12 @@
 // Tasks are ordered by instance and cut into GROUPS of at most kGroup tasks of
 // one instance.
 //
-// Scheduling: every warp of the grid is a worker.  Warp w starts on task w and
-// then takes the next task from a counter of the side (one atomic per task),
-// so the work spreads over the SMs as it runs instead of by a static split.
+// Scheduling: every warp of the grid is a worker over the side's ACTIVE task
+// list (the tasks of the instances still running, rebuilt after every
+// evaluation).  Warp w starts on entry w and then takes the next entry from a
+// counter of the side (one atomic per task), so the work spreads over the SMs
+// as it runs instead of by a static split (see task_loop for how a launch
+// tells its own counter values apart without a reset).
 // Reductions stay deterministic: a task's lanes reduce their compensated
 // accumulators (Acc) in a fixed butterfly into the task's slot; the warp that
 // completes a group (ticket) reduces the group's task slots in task order; the
@@ -297,11 +300,18 @@ template <int Q, class Epi, class Body>
 __device__ __forceinline__ void task_loop(const Side& side, Inst* st, Epi& epi, unsigned max_mask, Body&& body) {
     const int lane = threadIdx.x & 31;
     const int nw = gridDim.x * (blockDim.x >> 5);
-    int ti = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    while (ti < side.ntasks) {
-        // the next task index is fetched while this task runs
+    const int nact = *side.nactive;  // tasks of the running instances
+    int pos = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    while (pos < nact) {
+        // the next position is fetched while this task runs.  Every launch
+        // takes exactly nact values from the counter (nact - nw positions
+        // beyond the static first ones, then one past-the-end value per warp
+        // that entered), and launches on a side never overlap, so the value
+        // modulo nact is this launch's own sequence number; the compaction
+        // after each evaluation zeroes the counter.
         int next = 0;
-        if (lane == 0) next = (int)atomicAdd(&side.counters[0], 1u) + nw;
+        if (lane == 0) next = (int)(atomicAdd(&side.counters[0], 1u) % (unsigned)nact) + nw;
+        const int ti = side.active[pos];
         const Task t = side.tasks[ti];
         Inst& S = st[t.inst];
         if (!S.done) {  // uniform over the warp; it only changes after the instance's last task
@@ -312,12 +322,7 @@ __device__ __forceinline__ void task_loop(const Side& side, Inst* st, Epi& epi, 
             if (task_complete<Q>(side, ti, t.inst, q, max_mask, tot) && lane == 0) epi.finish(S, tot);
             __syncwarp();
         }
-        ti = __shfl_sync(FULL_MASK, next, 0);
-    }
-    // the last warp to leave resets the counters for the next launch
-    if (lane == 0 && atomicAdd(&side.counters[1], 1u) + 1u == (unsigned)nw) {
-        side.counters[0] = 0u;
-        side.counters[1] = 0u;
+        pos = __shfl_sync(FULL_MASK, next, 0);
     }
 }
 
@@ -340,8 +345,9 @@ __device__ __forceinline__ void spmv_engine(const Side& side, Inst* st, Epi& epi
 // instance, threads stride through a chunk (coalesced).
 template <class F>
 __device__ __forceinline__ void for_each_element(const Chunks& ch, Inst* st, F&& f) {
-    for (int c = blockIdx.x; c < ch.n; c += gridDim.x) {
-        const int4 d = ch.chunks[c];  // begin, end, instance, is_col
+    const int nact = *ch.nactive;
+    for (int c = blockIdx.x; c < nact; c += gridDim.x) {
+        const int4 d = ch.chunks[ch.active[c]];  // begin, end, instance, is_col
         const Inst& S = st[d.z];
         if (S.done) continue;
         const bool is_col = d.w != 0;

@@ -181,7 +181,9 @@ def _refinery_template(rng: np.random.Generator):
     add(_C_HDT_DIST, _R_COMP + 4, 1.0); add(_C_HDT_DIST, _R_HDT_FEED, -1.0)
     add(_C_HDT_CYC, _R_COMP + 6, 1.0); add(_C_HDT_CYC, _R_HDT_FEED, -1.0)
 
-    # component qualities: two octane-like (80..100) and two sulphur-like (0..50 ppm)
+    # component qualities: two octane-like (80..100) and two sulphur-like (0..50 ppm);
+    # a quality row is sum_k (q_k - spec) flow_k >= 0 (octane) or <= 0 (sulphur),
+    # the form of the reference builder (model_builder.py:271-290)
     octane = rng.uniform(80.0, 100.0, (_COMPONENTS, 2))
     sulphur = rng.uniform(0.0, 50.0, (_COMPONENTS, 2))
     grades = []   # (prod_col, sell_col, inv_col, tank_row)
@@ -194,8 +196,6 @@ def _refinery_template(rng: np.random.Generator):
             sul_spec = rng.uniform(10.0, 40.0, 2)
             prod, sell, inv = col, col + 1, col + 2
             add(prod, blend, -1.0)
-            add(prod, q0, -oct_spec[0]); add(prod, q1, -oct_spec[1])
-            add(prod, s0, -sul_spec[0]); add(prod, s1, -sul_spec[1])
             add(prod, tank, 1.0)
             add(sell, tank, -1.0)
             add(inv, tank, -1.0)
@@ -205,8 +205,8 @@ def _refinery_template(rng: np.random.Generator):
                 f = col + 3 + j
                 add(f, _R_COMP + int(k), 1.0)
                 add(f, blend, 1.0)
-                add(f, q0, octane[k, 0]); add(f, q1, octane[k, 1])
-                add(f, s0, sulphur[k, 0]); add(f, s1, sulphur[k, 1])
+                add(f, q0, octane[k, 0] - oct_spec[0]); add(f, q1, octane[k, 1] - oct_spec[1])
+                add(f, s0, sulphur[k, 0] - sul_spec[0]); add(f, s1, sulphur[k, 1] - sul_spec[1])
             grades.append((prod, sell, inv, tank))
             col += 3 + allowed.shape[0]
             row += 6
