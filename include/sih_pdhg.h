@@ -112,7 +112,8 @@ typedef struct sih_pdhg_options {
     int32_t compensated;       /* mixed: 0 off, 1 on near tolerance (default), 2 always */
     int32_t dual_sign;         /* 0 = PDHG sign of the reference (row_duals = -simplex duals), 1 = simplex sign */
     int32_t use_graph;         /* 1 = replay iteration blocks as CUDA graphs */
-    int32_t autotune;          /* 1 = time SpMV tile shapes once per matrix shape and keep the fastest */
+    int32_t autotune;          /* mixed: 1 = time the SpMV task sizes once per batch shape (instances, rows,
+                                  columns, nonzeros) at creation and keep the fastest (cached per process) */
     int32_t verbose;           /* 0 */
     double time_limit_sec;     /* <= 0: none */
     double restart_sufficient; /* mixed: 0.2 */
@@ -218,6 +219,18 @@ int sih_pdhg_get_result(sih_pdhg_handle* h, int32_t index, sih_pdhg_result* resu
  * step, [1] the A x step (rows), [2] the A^T y step (columns); bytes[0..2] get
  * each kernel's algorithmic bytes per launch.  The state is reset by the next run. */
 int sih_pdhg_time_kernels(sih_pdhg_handle* h, int32_t reps, double* seconds, double* bytes);
+/* Warm start of instance `index` for the following runs (mixed algorithm): x
+ * [n] in the original column order and row_duals [m] (may be NULL: zero) in the
+ * convention of the returned row_duals (options.dual_sign); primal_weight > 0
+ * also replaces the initial primal weight (e.g. the previous result's
+ * final_primal_weight).  x == NULL clears the start.  The re-solve caller of
+ * the reference (py/refinery/reoptimization.py:81-150) warm-starts its simplex
+ * the same way; the reference PDHG has no warm start. */
+int sih_pdhg_set_start(sih_pdhg_handle* h, int32_t index, const double* x, const double* row_duals,
+                       double primal_weight);
+/* Nonzeros per SpMV task in use (mixed algorithm; the autotuner's choice with
+ * options.autotune = 1). */
+int sih_pdhg_get_task_nnz(const sih_pdhg_handle* h, int32_t* task_nnz);
 void sih_pdhg_destroy(sih_pdhg_handle* h);
 
 /* One-call batch: create + run + result for each instance + destroy.

@@ -110,6 +110,20 @@ int sih_pdhg_time_kernels(sih_pdhg_handle* h, int32_t reps, double* seconds, dou
     return h->mixed->time_kernels(reps, seconds, bytes);
 }
 
+int sih_pdhg_set_start(sih_pdhg_handle* h, int32_t index, const double* x, const double* row_duals,
+                       double primal_weight) {
+    if (!h) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "NULL handle");
+    if (!h->mixed) return fail(SIH_PDHG_ERR_UNSUPPORTED, "warm starts are available for the mixed algorithm");
+    return h->mixed->set_start(index, x, row_duals, primal_weight);
+}
+
+int sih_pdhg_get_task_nnz(const sih_pdhg_handle* h, int32_t* task_nnz) {
+    if (!h || !task_nnz) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!h->mixed) return fail(SIH_PDHG_ERR_UNSUPPORTED, "task sizes belong to the mixed algorithm");
+    *task_nnz = h->mixed->task_nnz();
+    return SIH_PDHG_OK;
+}
+
 void sih_pdhg_destroy(sih_pdhg_handle* h) { delete h; }
 
 int sih_pdhg_solve_batch(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,

@@ -31,6 +31,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "mixed.h"
 #include "warp.cuh"
@@ -547,7 +550,7 @@ __global__ void k_init_controller(int B, Inst* st, double step_scale) {
     Inst& S = st[b];
     S.eta = S.kmax > 0.0 ? step_scale / S.kmax : 1.0;
     const double cn = sqrt(S.c2), bn = sqrt(S.b2);
-    S.omega = (cn > 1e-10 && bn > 1e-10) ? cn / bn : 1.0;
+    S.omega = S.omega_start > 0.0 ? S.omega_start : ((cn > 1e-10 && bn > 1e-10) ? cn / bn : 1.0);
 }
 
 // Initial point x = clip(0, l~, u~) in both buffers, as the average and as the
@@ -569,6 +572,28 @@ __global__ void k_init_point(int N, int M, Vecs V) {
         V.y_avg[i] = 0.f;
         V.y_last[i] = 0.f;
         V.y_acc[i] = make_float2(0.f, 0.f);
+    }
+}
+
+// Warm start of one instance: staged unscaled x (columns [c0, c1)) and y (rows
+// [r0, r1)) in the x1 / y1 buffers become the scaled start point
+// x~ = clip(x / dcol, l~, u~), y~ = y / drow, in every copy the initial point has.
+__global__ void k_apply_start(int c0, int c1, int r0, int r1, Vecs V) {
+    for (int j = c0 + blockIdx.x * blockDim.x + threadIdx.x; j < c1; j += gridDim.x * blockDim.x) {
+        const float x = fminf(fmaxf(V.x1[j] / V.dcol[j], V.l[j]), V.u[j]);
+        V.x0[j] = x;
+        V.x1[j] = x;
+        V.x_avg[j] = x;
+        V.x_last[j] = x;
+        V.x_acc[j] = make_float2(x, 0.f);
+    }
+    for (int i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += gridDim.x * blockDim.x) {
+        const float y = V.y1[i] / V.drow[i];
+        V.y0[i] = y;
+        V.y1[i] = y;
+        V.y_avg[i] = y;
+        V.y_last[i] = y;
+        V.y_acc[i] = make_float2(y, 0.f);
     }
 }
 
@@ -776,6 +801,105 @@ static int upload(DevMem& d, const void* h, size_t bytes, cudaStream_t s) {
     return SIH_PDHG_OK;
 }
 
+// Tasks, reduction groups, tickets, element chunks and active lists for SpMV
+// tasks of about `task_nnz` nonzeros (rebuilt by the autotuner).
+int MixedSolver::build_schedules(int task_nnz) {
+    cudaStream_t s = stream_;
+    task_nnz_ = task_nnz;
+    SideSchedule rs, cs;
+    make_schedule(h_csr_ptr_, row_off_, task_nnz_, rs);
+    make_schedule(h_csc_ptr_, col_off_, task_nnz_, cs);
+    // per side: tickets [B] + counters [2] + group tickets [ngroups], zeroed once;
+    // the kernels leave them zero
+    const size_t ng_r = rs.group_begin.size() - 1, ng_c = cs.group_begin.size() - 1;
+    const size_t nticket = 2 * ((size_t)B_ + 2) + ng_r + ng_c;
+    SIHG_TRY(tickets_.alloc(sizeof(unsigned) * nticket));
+    SIHG_CUDA(cudaMemsetAsync(tickets_.as<void>(), 0, sizeof(unsigned) * nticket, s));
+    auto upload_schedule = [&](const SideSchedule& sc, DevMem& mem, const SegMatrix& A, DevMem& part,
+                               unsigned* tick, Side& side) -> int {
+        const size_t nt = sc.tasks.size(), ng = sc.group_begin.size() - 1;
+        const size_t bytes = sizeof(Task) * nt +
+                             sizeof(int) * (sc.list_idx.size() + sc.light_max.size() + sc.task_group.size() +
+                                            sc.group_begin.size() + sc.inst_group_begin.size() +
+                                            sc.inst_task_begin.size()) + 112;
+        std::vector<char> buf(bytes, 0);
+        size_t off = 0;
+        auto put = [&](const void* src, size_t n) {
+            const size_t at = off;
+            if (n) std::memcpy(buf.data() + off, src, n);
+            off += (n + 15) & ~(size_t)15;
+            return at;
+        };
+        const size_t o_t = put(sc.tasks.data(), sizeof(Task) * nt);
+        const size_t o_h = put(sc.list_idx.data(), sizeof(int) * sc.list_idx.size());
+        const size_t o_x = put(sc.light_max.data(), sizeof(int) * sc.light_max.size());
+        const size_t o_g = put(sc.task_group.data(), sizeof(int) * sc.task_group.size());
+        const size_t o_b = put(sc.group_begin.data(), sizeof(int) * sc.group_begin.size());
+        const size_t o_i = put(sc.inst_group_begin.data(), sizeof(int) * sc.inst_group_begin.size());
+        const size_t o_s = put(sc.inst_task_begin.data(), sizeof(int) * sc.inst_task_begin.size());
+        buf.resize(std::max<size_t>(off, 16));
+        SIHG_TRY(upload(mem, buf.data(), buf.size(), s));
+        SIHG_TRY(part.alloc(sizeof(float2) * kQ * (std::max<size_t>(1, nt) + std::max<size_t>(1, ng))));
+        char* d = mem.as<char>();
+        float2* tp = part.as<float2>();
+        side = Side{A,
+                    (const Task*)(d + o_t),
+                    (int)nt,
+                    (const int*)(d + o_h),
+                    (const int*)(d + o_x),
+                    (const int*)(d + o_g),
+                    (const int*)(d + o_b),
+                    (const int*)(d + o_i),
+                    tp,
+                    tp + (size_t)kQ * std::max<size_t>(1, nt),
+                    tick + B_ + 2,  // group tickets
+                    tick,           // instance tickets
+                    tick + B_,      // counters
+                    (const int*)(d + o_s),
+                    nullptr,
+                    nullptr};
+        return SIH_PDHG_OK;
+    };
+    unsigned* tk = tickets_.as<unsigned>();
+    SIHG_TRY(upload_schedule(rs, row_sched_, SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()}, row_part_, tk,
+                             rows_));
+    SIHG_TRY(upload_schedule(cs, col_sched_, SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, col_part_,
+                             tk + B_ + 2 + ng_r, cols_));
+    {
+        std::vector<int4> ch;
+        std::vector<int> ch_begin(B_ + 1, 0);
+        for (int b = 0; b < B_; ++b) {
+            ch_begin[b] = (int)ch.size();
+            for (int side = 0; side < 2; ++side) {
+                const std::vector<int>& off = side == 0 ? col_off_ : row_off_;
+                for (int e0 = off[b]; e0 < off[b + 1]; e0 += kChunk)
+                    ch.push_back(make_int4(e0, std::min(off[b + 1], e0 + kChunk), b, side == 0 ? 1 : 0));
+            }
+        }
+        ch_begin[B_] = (int)ch.size();
+        const size_t nch = ch.size();
+        // chunk descriptors, then the chunk instance index
+        std::vector<char> buf(sizeof(int4) * std::max<size_t>(1, nch) + sizeof(int) * (B_ + 1), 0);
+        std::memcpy(buf.data(), ch.data(), sizeof(int4) * nch);
+        std::memcpy(buf.data() + sizeof(int4) * std::max<size_t>(1, nch), ch_begin.data(), sizeof(int) * (B_ + 1));
+        SIHG_TRY(upload(chunks_, buf.data(), buf.size(), s));
+        // active lists: rows tasks, cols tasks, chunks; 3 counts; 3 x B offsets
+        const size_t nr = rows_.ntasks, nc = cols_.ntasks;
+        SIHG_TRY(active_.alloc(sizeof(int) * (nr + nc + nch + 3 + 3 * (size_t)B_ + 8)));
+        int* a = active_.as<int>();
+        rows_.active = a;
+        cols_.active = a + nr;
+        int* cnt = a + nr + nc + nch;
+        rows_.nactive = cnt;
+        cols_.nactive = cnt + 1;
+        chunks_all_ = Chunks{chunks_.as<int4>(), (int)nch,
+                             (const int*)(chunks_.as<char>() + sizeof(int4) * std::max<size_t>(1, nch)),
+                             a + nr + nc, cnt + 2};
+    }
+
+    return SIH_PDHG_OK;
+}
+
 int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_pdhg_config& cfg,
                        const sih_pdhg_options& opts) {
     probs_ = probs;
@@ -895,101 +1019,13 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     task_nnz_ = opts.tile_nnz > 0 ? opts.tile_nnz
                                   : (int)std::max(128LL, std::min(2048LL, nnz / std::max(1LL, 3 * warps)));
     task_nnz_ = std::max(32, std::min(1 << 20, task_nnz_));
-    SideSchedule rs, cs;
-    make_schedule(csr_ptr, row_off_, task_nnz_, rs);
-    make_schedule(csc_ptr, col_off_, task_nnz_, cs);
-
     SIHG_TRY(upload(csr_ptr_, csr_ptr.data(), sizeof(int) * csr_ptr.size(), s));
     SIHG_TRY(upload(csc_ptr_, csc_ptr.data(), sizeof(int) * csc_ptr.size(), s));
     SIHG_TRY(upload(csr_pairs_, csr.data(), sizeof(Pair) * csr.size(), s));
     SIHG_TRY(upload(csc_pairs_, csc.data(), sizeof(Pair) * csc.size(), s));
-    // per side: tickets [B] + counters [2] + group tickets [ngroups], zeroed once;
-    // the kernels leave them zero
-    const size_t ng_r = rs.group_begin.size() - 1, ng_c = cs.group_begin.size() - 1;
-    const size_t nticket = 2 * ((size_t)B_ + 2) + ng_r + ng_c;
-    SIHG_TRY(tickets_.alloc(sizeof(unsigned) * nticket));
-    SIHG_CUDA(cudaMemsetAsync(tickets_.as<void>(), 0, sizeof(unsigned) * nticket, s));
-    auto upload_schedule = [&](const SideSchedule& sc, DevMem& mem, const SegMatrix& A, DevMem& part,
-                               unsigned* tick, Side& side) -> int {
-        const size_t nt = sc.tasks.size(), ng = sc.group_begin.size() - 1;
-        const size_t bytes = sizeof(Task) * nt +
-                             sizeof(int) * (sc.list_idx.size() + sc.light_max.size() + sc.task_group.size() +
-                                            sc.group_begin.size() + sc.inst_group_begin.size() +
-                                            sc.inst_task_begin.size()) + 112;
-        std::vector<char> buf(bytes, 0);
-        size_t off = 0;
-        auto put = [&](const void* src, size_t n) {
-            const size_t at = off;
-            if (n) std::memcpy(buf.data() + off, src, n);
-            off += (n + 15) & ~(size_t)15;
-            return at;
-        };
-        const size_t o_t = put(sc.tasks.data(), sizeof(Task) * nt);
-        const size_t o_h = put(sc.list_idx.data(), sizeof(int) * sc.list_idx.size());
-        const size_t o_x = put(sc.light_max.data(), sizeof(int) * sc.light_max.size());
-        const size_t o_g = put(sc.task_group.data(), sizeof(int) * sc.task_group.size());
-        const size_t o_b = put(sc.group_begin.data(), sizeof(int) * sc.group_begin.size());
-        const size_t o_i = put(sc.inst_group_begin.data(), sizeof(int) * sc.inst_group_begin.size());
-        const size_t o_s = put(sc.inst_task_begin.data(), sizeof(int) * sc.inst_task_begin.size());
-        buf.resize(std::max<size_t>(off, 16));
-        SIHG_TRY(upload(mem, buf.data(), buf.size(), s));
-        SIHG_TRY(part.alloc(sizeof(float2) * kQ * (std::max<size_t>(1, nt) + std::max<size_t>(1, ng))));
-        char* d = mem.as<char>();
-        float2* tp = part.as<float2>();
-        side = Side{A,
-                    (const Task*)(d + o_t),
-                    (int)nt,
-                    (const int*)(d + o_h),
-                    (const int*)(d + o_x),
-                    (const int*)(d + o_g),
-                    (const int*)(d + o_b),
-                    (const int*)(d + o_i),
-                    tp,
-                    tp + (size_t)kQ * std::max<size_t>(1, nt),
-                    tick + B_ + 2,  // group tickets
-                    tick,           // instance tickets
-                    tick + B_,      // counters
-                    (const int*)(d + o_s),
-                    nullptr,
-                    nullptr};
-        return SIH_PDHG_OK;
-    };
-    unsigned* tk = tickets_.as<unsigned>();
-    SIHG_TRY(upload_schedule(rs, row_sched_, SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()}, row_part_, tk,
-                             rows_));
-    SIHG_TRY(upload_schedule(cs, col_sched_, SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, col_part_,
-                             tk + B_ + 2 + ng_r, cols_));
-    {
-        std::vector<int4> ch;
-        std::vector<int> ch_begin(B_ + 1, 0);
-        for (int b = 0; b < B_; ++b) {
-            ch_begin[b] = (int)ch.size();
-            for (int side = 0; side < 2; ++side) {
-                const std::vector<int>& off = side == 0 ? col_off_ : row_off_;
-                for (int e0 = off[b]; e0 < off[b + 1]; e0 += kChunk)
-                    ch.push_back(make_int4(e0, std::min(off[b + 1], e0 + kChunk), b, side == 0 ? 1 : 0));
-            }
-        }
-        ch_begin[B_] = (int)ch.size();
-        const size_t nch = ch.size();
-        // chunk descriptors, then the chunk instance index
-        std::vector<char> buf(sizeof(int4) * std::max<size_t>(1, nch) + sizeof(int) * (B_ + 1), 0);
-        std::memcpy(buf.data(), ch.data(), sizeof(int4) * nch);
-        std::memcpy(buf.data() + sizeof(int4) * std::max<size_t>(1, nch), ch_begin.data(), sizeof(int) * (B_ + 1));
-        SIHG_TRY(upload(chunks_, buf.data(), buf.size(), s));
-        // active lists: rows tasks, cols tasks, chunks; 3 counts; 3 x B offsets
-        const size_t nr = rows_.ntasks, nc = cols_.ntasks;
-        SIHG_TRY(active_.alloc(sizeof(int) * (nr + nc + nch + 3 + 3 * (size_t)B_ + 8)));
-        int* a = active_.as<int>();
-        rows_.active = a;
-        cols_.active = a + nr;
-        int* cnt = a + nr + nc + nch;
-        rows_.nactive = cnt;
-        cols_.nactive = cnt + 1;
-        chunks_all_ = Chunks{chunks_.as<int4>(), (int)nch,
-                             (const int*)(chunks_.as<char>() + sizeof(int4) * std::max<size_t>(1, nch)),
-                             a + nr + nc, cnt + 2};
-    }
+    h_csr_ptr_ = std::move(csr_ptr);
+    h_csc_ptr_ = std::move(csc_ptr);
+    SIHG_TRY(build_schedules(task_nnz_));
 
     // ---- vectors: 11 column vectors, 10 row vectors (layout of Vecs) + float-float averages
     SIHG_TRY(colvec_.alloc(sizeof(float) * (size_t)N_ * 11));
@@ -1061,6 +1097,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
         S.beta_art = opts.restart_artificial;
         S.weight_smoothing = opts.primal_weight_smoothing;
     }
+    if (opts.autotune && opts.tile_nnz <= 0) SIHG_TRY(autotune());
     return SIH_PDHG_OK;
 }
 
@@ -1120,7 +1157,22 @@ int MixedSolver::reset_state() {
     // initial point x = clip(0, l~, u~), y = 0; averages and last points equal it
     k_init_point<<<g, 256, 0, s>>>(N_, M_, V_);
     SIHG_LAUNCH_CHECK();
+    bool warm = false;
+    for (int b = 0; b < B_; ++b) {
+        if (start_x_.size() <= (size_t)b || start_x_[b].empty()) continue;
+        warm = true;
+        const int co = col_off_[b], ro = row_off_[b], n = probs_[b]->n, m = probs_[b]->m;
+        SIHG_CUDA(cudaMemcpyAsync(V_.x1 + co, start_x_[b].data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
+        SIHG_CUDA(cudaMemcpyAsync(V_.y1 + ro, start_y_[b].data(), sizeof(float) * m, cudaMemcpyHostToDevice, s));
+        k_apply_start<<<std::max(1, std::min(g, (std::max(n, m) + 255) / 256)), 256, 0, s>>>(co, co + n, ro, ro + m, V_);
+        launches_ += 1;
+    }
+    SIHG_LAUNCH_CHECK();
     k_spmv_store<<<grid_, kThreads, 0, s>>>(rows_, state_.as<Inst>(), V_.x0, V_.kx0);
+    if (warm) {  // K^T y of the start point (zero for a cold start)
+        k_spmv_store<<<grid_, kThreads, 0, s>>>(cols_, state_.as<Inst>(), V_.y0, V_.kty0);
+        launches_ += 1;
+    }
     k_init_stats_rows<<<grid_, kThreads, 0, s>>>(rows_, V_, state_.as<Inst>());
     k_init_stats_cols<<<grid_, kThreads, 0, s>>>(cols_, V_, state_.as<Inst>());
     k_init_controller<<<(B_ + 127) / 128, 128, 0, s>>>(B_, state_.as<Inst>(), 1.0);
@@ -1261,6 +1313,84 @@ int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
         bytes[2] = 8.0 * nnz + 4.0 * (n + 1) + 4.0 * m + 16.0 * n;  // pairs, ptr, y' gathered, column epilogue
     }
     return rc;
+}
+
+// Start point for instance b from the next run on: x (original column order)
+// and y (original row order, in the convention of the returned row_duals,
+// options.dual_sign); omega > 0 also sets the initial primal weight.  NULL x
+// clears the start.
+int MixedSolver::set_start(int b, const double* x, const double* y, double omega) {
+    if (b < 0 || b >= B_) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "instance index out of range");
+    start_x_.resize(B_);
+    start_y_.resize(B_);
+    if (!x) {
+        start_x_[b].clear();
+        start_y_[b].clear();
+        host_inst_[b].omega_start = 0.0;
+        return SIH_PDHG_OK;
+    }
+    const int n = probs_[b]->n, m = probs_[b]->m, co = col_off_[b], ro = row_off_[b];
+    start_x_[b].assign(n, 0.f);
+    start_y_[b].assign(m, 0.f);
+    for (int j = 0; j < n; ++j) {
+        const double v = x[col_perm_[co + j]];
+        if (!std::isfinite(v)) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "start x is not finite");
+        start_x_[b][j] = (float)v;
+    }
+    for (int i = 0; i < m; ++i) {
+        const double v = y ? y[row_perm_[ro + i]] : 0.0;
+        if (!std::isfinite(v)) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "start y is not finite");
+        // same convention as the returned row_duals (options.dual_sign)
+        start_y_[b][i] = (float)(opts_.dual_sign ? -v * probs_[b]->sense : v);
+    }
+    host_inst_[b].omega_start = omega > 0.0 && std::isfinite(omega) ? omega : 0.0;
+    return SIH_PDHG_OK;
+}
+
+// SpMV task-size autotuner (options.autotune): times the two SpMV step
+// kernels for a ladder of task sizes on this batch and keeps the fastest.  The
+// choice is cached per process for the shape (instances, rows, columns,
+// nonzeros), so repeated solves of one shape tune once.
+int MixedSolver::autotune() {
+    struct Key {
+        int b, m, n;
+        long long nnz;
+        bool operator<(const Key& o) const {
+            return std::tie(b, m, n, nnz) < std::tie(o.b, o.m, o.n, o.nnz);
+        }
+    };
+    static std::mutex mu;
+    static std::map<Key, int> cache;
+    const Key key{B_, M_, N_, nnz_};
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            if (it->second != task_nnz_) SIHG_TRY(build_schedules(it->second));
+            return SIH_PDHG_OK;
+        }
+    }
+    std::vector<int> ladder = {256, 384, 512, 768, 1024, 1536, 2048, task_nnz_};
+    std::sort(ladder.begin(), ladder.end());
+    ladder.erase(std::unique(ladder.begin(), ladder.end()), ladder.end());
+    int best = task_nnz_;
+    double best_t = INFINITY;
+    const int reps = nnz_ > 4000000 ? 5 : 20;
+    for (int t : ladder) {
+        if ((long long)t > std::max<long long>(nnz_, 256)) continue;
+        SIHG_TRY(build_schedules(t));
+        double sec[3];
+        SIHG_TRY(time_kernels(reps, sec, nullptr));
+        const double spmv = sec[1] + sec[2];
+        if (spmv < best_t) {
+            best_t = spmv;
+            best = t;
+        }
+    }
+    SIHG_TRY(build_schedules(best));
+    std::lock_guard<std::mutex> g(mu);
+    cache[key] = best;
+    return SIH_PDHG_OK;
 }
 
 int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,

@@ -55,6 +55,7 @@ struct Inst {
     double b_inf, c_inf, tol_p, tol_d, tol_g;
     double beta_suff, beta_nec, beta_art, weight_smoothing;
     double kmax, b2, c2;
+    double omega_start;  // > 0: initial primal weight of a warm start
 };
 
 struct Side {
@@ -131,12 +132,16 @@ class MixedSolver {
     int launch_eval(cudaStream_t s);
     // Times `reps` launches of each step kernel (elementwise, rows, columns).
     int time_kernels(int reps, double* seconds, double* bytes);
+    int set_start(int b, const double* x, const double* y, double omega);
+    int task_nnz() const { return task_nnz_; }
     long long nnz() const { return nnz_; }
     int rows() const { return M_; }
     int cols() const { return N_; }
 
   private:
     int reset_state();
+    int build_schedules(int task_nnz);
+    int autotune();
     int launch_compact(cudaStream_t s);
     int record_graph();
 
@@ -157,6 +162,7 @@ class MixedSolver {
     cudaGraphExec_t graphs_[1] = {nullptr};
     std::vector<int> row_off_, col_off_;
     std::vector<int> col_perm_, row_perm_;  // device order -> instance-local original index
+    std::vector<int> h_csr_ptr_, h_csc_ptr_;  // segment pointers (device order), for schedule rebuilds
     DevMem csr_ptr_, csc_ptr_, csr_pairs_, csc_pairs_, row_sched_, col_sched_;
     DevMem row_part_, col_part_, tickets_, colvec_, rowvec_, state_, done_count_, accvec_, chunks_, active_;
     Side rows_{}, cols_{};
@@ -164,6 +170,7 @@ class MixedSolver {
     int elem_grid_ = 1;
     Vecs V_{};
     std::vector<Inst> host_inst_;
+    std::vector<std::vector<float>> start_x_, start_y_;  // warm starts (device order, unscaled)
 };
 
 int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,

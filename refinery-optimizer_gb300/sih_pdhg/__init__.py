@@ -107,6 +107,28 @@ class PdhgHandle:
         _lib.check(self._lib.sih_pdhg_time_kernels(self._h, reps, secs, byts))
         return list(secs), list(byts)
 
+    def set_start(self, index: int, x, row_duals=None, primal_weight: float = 0.0) -> None:
+        """Warm start of instance `index` for the following runs (x in the
+        original column order, row_duals in the returned convention; None
+        clears it).  Pass a previous Solution's x, row_duals and
+        final_primal_weight to re-solve a perturbed scenario."""
+        if x is None:
+            _lib.check(self._lib.sih_pdhg_set_start(self._h, index, None, None, 0.0))
+            return
+        xa = np.ascontiguousarray(x, dtype=np.float64)
+        ya = None if row_duals is None else np.ascontiguousarray(row_duals, dtype=np.float64)
+        p = self.problems[index] if 0 <= index < len(self.problems) else None
+        if p is not None and (xa.shape != (p.num_cols(),) or (ya is not None and ya.shape != (p.num_rows(),))):
+            raise SihPdhgError(1, "start vectors do not match the instance's shape")
+        _lib.check(self._lib.sih_pdhg_set_start(self._h, index, xa.ctypes.data,
+                                                None if ya is None else ya.ctypes.data, float(primal_weight)))
+
+    def task_nnz(self) -> int:
+        """Nonzeros per SpMV task in use (the autotuner's choice with autotune=1)."""
+        v = C.c_int32()
+        _lib.check(self._lib.sih_pdhg_get_task_nnz(self._h, C.byref(v)))
+        return v.value
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.sih_pdhg_destroy(self._h)

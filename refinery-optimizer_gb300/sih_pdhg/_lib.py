@@ -93,6 +93,8 @@ def load() -> C.CDLL:
     lib.sih_pdhg_run.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     lib.sih_pdhg_get_result.argtypes = [C.c_void_p, C.c_int32, C.POINTER(CResult)]
     lib.sih_pdhg_time_kernels.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.sih_pdhg_set_start.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double]
+    lib.sih_pdhg_get_task_nnz.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     lib.sih_pdhg_destroy.argtypes = [C.c_void_p]
     lib.sih_pdhg_destroy.restype = None
     lib.sih_pdhg_check_norms_noalloc.argtypes = [i32, i32, i32] + [vp] * 14 + [C.c_float, C.c_float, vp, vp]
