@@ -265,6 +265,64 @@ int sih_pdhg_launch_residuals(int m, int n, const float* d_Ax, const float* d_ro
                               const float* d_l, const float* d_u, const float* d_tau, float* d_col_viols,
                               void* stream);
 
+/* ---- adjoint (differentiation of the LP solution map) ---------------------
+ * No counterpart in the reference (its docs/gpu_pdhg.md plans a differentiable
+ * LP layer; the code has none).  Given solved LPs (x, row_duals as returned by
+ * this library with options.dual_sign 0) and the gradient of a loss with
+ * respect to x, returns the loss gradient with respect to the objective
+ * (zero: an LP solution does not move under small cost changes), the row
+ * bounds and the column bounds.  The active pattern of the PDHG fixed point
+ * is read off (x, y) as a basis (the m variables with the largest
+ * primal-slack / dual-slack ratio) and the adjoint system B^T lambda = dL/dx_F
+ * of the active rows and free columns is solved on the GPU by CGLS with the
+ * engine's SpMV kernels.  An equality row's gradient goes to grad_row_lower.
+ * Each pointer array has `count` entries; any output array may be NULL. */
+typedef struct sih_pdhg_adjoint_options {
+    int32_t struct_size;     /* sizeof(sih_pdhg_adjoint_options) */
+    int32_t reserved;
+    double tolerance;        /* CGLS stop: normal-equation residual <= tolerance x its initial value (1e-6) */
+    int64_t max_iterations;  /* CGLS iterations per instance; 0 = 20 (m + n) + 1000 */
+} sih_pdhg_adjoint_options;
+
+typedef struct sih_pdhg_adjoint_info {
+    int32_t status;          /* 0 converged, 1 iteration limit */
+    int32_t reserved;
+    int64_t iterations;      /* CGLS iterations over all refinement rounds */
+    double residual;         /* |dL/dx_F - B^T lambda| / |dL/dx_F| in FP64 after the refinement rounds */
+    int64_t free_columns;    /* columns of the basis */
+    int64_t active_rows;     /* rows whose slack is non-basic (at a bound) */
+} sih_pdhg_adjoint_info;
+
+typedef struct sih_pdhg_polish_info {
+    int32_t status;            /* 0 both systems converged, 1 an iteration limit was hit */
+    int32_t reserved;
+    int64_t iterations;        /* CGLS iterations, both systems */
+    double primal_residual;    /* |b_act - B x_F| / |b_act| (FP64) */
+    double dual_residual;      /* |c_F - B^T lambda| / |c_F| (FP64) */
+    double primal_violation;   /* max bound violation of the vertex (rows and columns) / max(1, |x|_inf) */
+    double dual_violation;     /* max wrong-sign reduced cost or row dual / max(1, |c|_inf): 0 = optimal basis */
+    int64_t free_columns;
+    int64_t active_rows;
+} sih_pdhg_polish_info;
+
+void sih_pdhg_adjoint_options_default(sih_pdhg_adjoint_options* opts);
+/* Basis polish (the GPU half of the reference's hybrid, gpu_solver.cpp:309-420,
+ * which ranks variables by distance to their bounds and hands the basis to the
+ * FP64 simplex): the basis read off (x, row_duals) as in sih_pdhg_adjoint_batch,
+ * then its vertex x_out (B x_F = b_act - A[act, N] x_N) and its duals
+ * row_duals_out (B^T lambda = c_F, PDHG sign as returned with dual_sign 0),
+ * both by CGLS on the GPU with FP64 refinement.  info reports the residuals
+ * and how far the vertex is from primal / dual feasibility (both zero: the
+ * basis is optimal and x_out is an exact optimal vertex). */
+int sih_pdhg_polish_batch(const sih_pdhg_problem* problems, int32_t count, const double* const* x,
+                          const double* const* row_duals, double* const* x_out, double* const* row_duals_out,
+                          const sih_pdhg_adjoint_options* opts, sih_pdhg_polish_info* info);
+int sih_pdhg_adjoint_batch(const sih_pdhg_problem* problems, int32_t count, const double* const* x,
+                           const double* const* row_duals, const double* const* grad_x, double* const* grad_c,
+                           double* const* grad_row_lower, double* const* grad_row_upper,
+                           double* const* grad_col_lower, double* const* grad_col_upper,
+                           const sih_pdhg_adjoint_options* opts, sih_pdhg_adjoint_info* info);
+
 /* ---- convergence check without allocation ---------------------------------
  * No counterpart in the reference.  For callers that must not allocate device
  * memory while they run (a host that hands every library a fixed device pool

@@ -37,7 +37,9 @@
 //   void apply(int seg, const SegDot<NV>&, const Pre&)
 //   void values(Acc (&q)[Q])                   this lane's partial reductions; resets them
 //                                              (a max travels in q.s with q.c = 0)
-//   void finish(Inst&, const double* total)    instance controller (one lane)
+//   void finish(State&, const double* total)   instance controller (one lane)
+// The per-instance state type (Inst for the PDHG solver) has `done` and
+// `refine` fields; a task of a done instance is skipped.
 #pragma once
 
 #include "mixed.h"
@@ -296,8 +298,8 @@ __device__ bool task_complete(const Side& side, int ti, int inst, Acc (&q)[Q], u
 
 // Worker loop of one warp over the side's tasks.  `body(t, S)` does the work
 // of one task (all lanes), leaving partials in `epi`.
-template <int Q, class Epi, class Body>
-__device__ __forceinline__ void task_loop(const Side& side, Inst* st, Epi& epi, unsigned max_mask, Body&& body) {
+template <int Q, class Epi, class State, class Body>
+__device__ __forceinline__ void task_loop(const Side& side, State* st, Epi& epi, unsigned max_mask, Body&& body) {
     const int lane = threadIdx.x & 31;
     const int nw = gridDim.x * (blockDim.x >> 5);
     const int nact = *side.nactive;  // tasks of the running instances
@@ -313,7 +315,7 @@ __device__ __forceinline__ void task_loop(const Side& side, Inst* st, Epi& epi, 
         if (lane == 0) next = (int)(atomicAdd(&side.counters[0], 1u) % (unsigned)nact) + nw;
         const int ti = side.active[pos];
         const Task t = side.tasks[ti];
-        Inst& S = st[t.inst];
+        State& S = st[t.inst];
         if (!S.done) {  // uniform over the warp; it only changes after the instance's last task
             body(t, S);
             Acc q[Q];
@@ -328,9 +330,9 @@ __device__ __forceinline__ void task_loop(const Side& side, Inst* st, Epi& epi, 
 
 // SpMV engine: the tasks of the side with the epilogue Epi.  With ALLOW_COMP
 // the tasks of an instance with `refine` set run compensated (Dot2).
-template <int NV, bool ALLOW_COMP, int Q, class Epi>
-__device__ __forceinline__ void spmv_engine(const Side& side, Inst* st, Epi& epi, unsigned max_mask) {
-    task_loop<Q>(side, st, epi, max_mask, [&](const Task& t, const Inst& S) {
+template <int NV, bool ALLOW_COMP, int Q, class Epi, class State>
+__device__ __forceinline__ void spmv_engine(const Side& side, State* st, Epi& epi, unsigned max_mask) {
+    task_loop<Q>(side, st, epi, max_mask, [&](const Task& t, const State& S) {
         epi.begin(S);
         const int lmax = side.light_max[t.inst];
         if (ALLOW_COMP && S.refine)
@@ -343,12 +345,12 @@ __device__ __forceinline__ void spmv_engine(const Side& side, Inst* st, Epi& epi
 // Elementwise pass over every column (is_col) and row of the running
 // instances: blocks take chunks of kChunk consecutive elements of one
 // instance, threads stride through a chunk (coalesced).
-template <class F>
-__device__ __forceinline__ void for_each_element(const Chunks& ch, Inst* st, F&& f) {
+template <class State, class F>
+__device__ __forceinline__ void for_each_element(const Chunks& ch, State* st, F&& f) {
     const int nact = *ch.nactive;
     for (int c = blockIdx.x; c < nact; c += gridDim.x) {
         const int4 d = ch.chunks[ch.active[c]];  // begin, end, instance, is_col
-        const Inst& S = st[d.z];
+        const State& S = st[d.z];
         if (S.done) continue;
         const bool is_col = d.w != 0;
         for (int r = d.x + threadIdx.x; r < d.y; r += blockDim.x) f(is_col, S, r);

@@ -22,7 +22,7 @@ from .problem import INF, ObjectiveSense, Problem, Solution, SolutionStatus, Spa
 
 __all__ = ["GpuSolver", "GpuPdhgConfig", "GpuMemoryInfo", "Problem", "SparseMatrix", "Solution",
            "SolutionStatus", "ObjectiveSense", "solve_gpu_pdhg", "solve_gpu_mixed", "solve_batch", "PdhgHandle",
-           "default_options", "SihPdhgError", "ALGO_PLAIN", "ALGO_MIXED", "INF"]
+           "default_options", "SihPdhgError", "ALGO_PLAIN", "ALGO_MIXED", "INF", "adjoint_batch", "polish_batch"]
 
 
 @dataclass
@@ -156,6 +156,70 @@ def solve_batch(problems, config: Optional[GpuPdhgConfig] = None, **options):
     res_arr = (_lib.CResult * len(problems))(*[o[0] for o in outs])
     _lib.check(lib.sih_pdhg_solve_batch(arr, len(views), C.byref(config), C.byref(opts), res_arr))
     return [_to_solution(res_arr[i], outs[i][1]) for i in range(len(problems))]
+
+
+def adjoint_batch(problems, xs, row_duals, grad_xs, tolerance: float = 1e-6, max_iterations: int = 0):
+    """Gradients of a loss with respect to the LP data, from the loss gradient
+    with respect to each solution x (sih_pdhg_adjoint_batch).  `row_duals` as
+    returned with the default dual_sign.  Returns (grads, infos): grads[i] is a
+    dict with c, row_lower, row_upper, col_lower, col_upper (float64 arrays)."""
+    lib = _lib.load()
+    problems = list(problems)
+    B = len(problems)
+    views = [_lib.c_problem(p) for p in problems]
+    arr = (_lib.CProblem * B)(*[v[0] for v in views])
+    keep = [v[1] for v in views]
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    xs = [f64(a) for a in xs]
+    ys = [f64(a) for a in row_duals]
+    gs = [f64(a) for a in grad_xs]
+    for p, x, y, g in zip(problems, xs, ys, gs):
+        if x.shape != (p.num_cols(),) or g.shape != (p.num_cols(),) or y.shape != (p.num_rows(),):
+            raise SihPdhgError(1, "x / grad_x need num_cols entries and row_duals num_rows")
+    out = [{k: np.zeros(p.num_cols() if k in ("c", "col_lower", "col_upper") else p.num_rows())
+            for k in ("c", "row_lower", "row_upper", "col_lower", "col_upper")} for p in problems]
+    ptrs = lambda lst: (C.c_void_p * B)(*[a.ctypes.data for a in lst])
+    opts = _lib.CAdjointOptions()
+    lib.sih_pdhg_adjoint_options_default(C.byref(opts))
+    opts.tolerance = float(tolerance)
+    opts.max_iterations = int(max_iterations)
+    infos = (_lib.CAdjointInfo * B)()
+    _lib.check(lib.sih_pdhg_adjoint_batch(
+        arr, B, ptrs(xs), ptrs(ys), ptrs(gs), ptrs([o["c"] for o in out]), ptrs([o["row_lower"] for o in out]),
+        ptrs([o["row_upper"] for o in out]), ptrs([o["col_lower"] for o in out]), ptrs([o["col_upper"] for o in out]),
+        C.byref(opts), infos))
+    del keep
+    return out, [{k: getattr(infos[i], k) for k, _ in _lib.CAdjointInfo._fields_ if k != "reserved"}
+                 for i in range(B)]
+
+
+def polish_batch(problems, xs, row_duals, tolerance: float = 1e-6, max_iterations: int = 0):
+    """Basis polish (sih_pdhg_polish_batch): the vertex and duals of the basis
+    read off each PDHG point.  Returns (xs_out, duals_out, infos)."""
+    lib = _lib.load()
+    problems = list(problems)
+    B = len(problems)
+    views = [_lib.c_problem(p) for p in problems]
+    arr = (_lib.CProblem * B)(*[v[0] for v in views])
+    keep = [v[1] for v in views]
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    xs = [f64(a) for a in xs]
+    ys = [f64(a) for a in row_duals]
+    for p, x, y in zip(problems, xs, ys):
+        if x.shape != (p.num_cols(),) or y.shape != (p.num_rows(),):
+            raise SihPdhgError(1, "x needs num_cols entries and row_duals num_rows")
+    xo = [np.zeros(p.num_cols()) for p in problems]
+    yo = [np.zeros(p.num_rows()) for p in problems]
+    ptrs = lambda lst: (C.c_void_p * B)(*[a.ctypes.data for a in lst])
+    opts = _lib.CAdjointOptions()
+    lib.sih_pdhg_adjoint_options_default(C.byref(opts))
+    opts.tolerance = float(tolerance)
+    opts.max_iterations = int(max_iterations)
+    infos = (_lib.CPolishInfo * B)()
+    _lib.check(lib.sih_pdhg_polish_batch(arr, B, ptrs(xs), ptrs(ys), ptrs(xo), ptrs(yo), C.byref(opts), infos))
+    del keep
+    return xo, yo, [{k: getattr(infos[i], k) for k, _ in _lib.CPolishInfo._fields_ if k != "reserved"}
+                    for i in range(B)]
 
 
 class GpuSolver:

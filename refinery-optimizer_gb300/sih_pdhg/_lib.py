@@ -49,6 +49,22 @@ class COptions(C.Structure):
                 ("tile_nnz", C.c_int32), ("reorder", C.c_int32)]
 
 
+class CAdjointOptions(C.Structure):
+    _fields_ = [("struct_size", C.c_int32), ("reserved", C.c_int32), ("tolerance", C.c_double),
+                ("max_iterations", C.c_int64)]
+
+
+class CAdjointInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("reserved", C.c_int32), ("iterations", C.c_int64), ("residual", C.c_double),
+                ("free_columns", C.c_int64), ("active_rows", C.c_int64)]
+
+
+class CPolishInfo(C.Structure):
+    _fields_ = [("status", C.c_int32), ("reserved", C.c_int32), ("iterations", C.c_int64),
+                ("primal_residual", C.c_double), ("dual_residual", C.c_double), ("primal_violation", C.c_double),
+                ("dual_violation", C.c_double), ("free_columns", C.c_int64), ("active_rows", C.c_int64)]
+
+
 class CResult(C.Structure):
     _fields_ = [("x", C.c_void_p), ("row_duals", C.c_void_p), ("slack", C.c_void_p),
                 ("reduced_costs", C.c_void_p), ("status", C.c_int32), ("reserved0", C.c_int32),
@@ -95,6 +111,12 @@ def load() -> C.CDLL:
     lib.sih_pdhg_time_kernels.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.sih_pdhg_set_start.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double]
     lib.sih_pdhg_get_task_nnz.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    lib.sih_pdhg_adjoint_options_default.argtypes = [C.c_void_p]
+    lib.sih_pdhg_adjoint_options_default.restype = None
+    pp = C.POINTER(C.c_void_p)
+    lib.sih_pdhg_adjoint_batch.argtypes = [C.c_void_p, C.c_int32, pp, pp, pp, pp, pp, pp, pp, pp, C.c_void_p,
+                                           C.c_void_p]
+    lib.sih_pdhg_polish_batch.argtypes = [C.c_void_p, C.c_int32, pp, pp, pp, pp, C.c_void_p, C.c_void_p]
     lib.sih_pdhg_destroy.argtypes = [C.c_void_p]
     lib.sih_pdhg_destroy.restype = None
     lib.sih_pdhg_check_norms_noalloc.argtypes = [i32, i32, i32] + [vp] * 14 + [C.c_float, C.c_float, vp, vp]

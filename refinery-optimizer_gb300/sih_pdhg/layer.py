@@ -1,0 +1,85 @@
+"""Differentiable LP layer: torch.autograd.Function over the GB300 engine.
+
+    x = lp_layer(matrices, c, row_lower, row_upper, col_lower, col_upper)
+
+Forward: one batched solve of the LPs
+    min c_i^T x  s.t.  row_lower_i <= A_i x <= row_upper_i,  col_lower_i <= x <= col_upper_i
+with the mixed-precision restarted adaptive PDHG (sih_pdhg_solve_batch), then
+the basis polish (sih_pdhg_polish_batch): the layer returns the vertex of the
+basis read off the PDHG point, the point whose neighbourhood the backward
+differentiates.
+Backward: the adjoint kernel (sih_pdhg_adjoint_batch): the active pattern of
+the PDHG fixed point read off (x*, y*) as a basis, and B^T lambda = dL/dx_F
+solved on the GPU by CGLS with the engine's SpMVs.  Gradients flow to the row
+bounds and column bounds; the objective's implicit gradient is zero (an LP
+solution is locally constant in c), so dL/dc is what the loss itself puts on c
+(for L = |x* - t|^2 + lam c^T x*, that is lam x*).
+
+Tensors are float64, shaped (batch, n) for c / col bounds and (batch, m) for
+row bounds, on any device (the solve copies them to the host); infinite bounds
+are +-inf.  The matrices (one sih_pdhg SparseMatrix per instance, all of the
+same shape) are constants of the layer.
+"""
+from __future__ import annotations
+
+from typing import List, Optional
+
+import numpy as np
+
+from . import adjoint_batch, polish_batch, solve_batch
+from .config import GpuPdhgConfig
+from .problem import ObjectiveSense, Problem, SparseMatrix
+
+try:
+    import torch
+except ImportError:  # the layer needs torch; the rest of the package does not
+    torch = None
+
+
+def _problems(mats: List[SparseMatrix], c, rl, ru, l, u) -> List[Problem]:
+    out = []
+    for i, A in enumerate(mats):
+        out.append(Problem.from_arrays(A, c[i], l[i], u[i], rl[i], ru[i], ObjectiveSense.Minimize, 0.0, f"layer{i}"))
+    return out
+
+
+if torch is not None:
+
+    class LPFunction(torch.autograd.Function):
+        """autograd.Function (c, row_lower, row_upper, col_lower, col_upper) -> x*."""
+
+        @staticmethod
+        def forward(ctx, c, row_lower, row_upper, col_lower, col_upper, mats, config, adjoint_tol):
+            host = [t.detach().to("cpu", torch.float64).numpy() for t in (c, row_lower, row_upper, col_lower,
+                                                                            col_upper)]
+            probs = _problems(mats, *host)
+            sols = solve_batch(probs, config)
+            for i, s in enumerate(sols):
+                if not s.is_optimal():
+                    raise RuntimeError(f"LP layer: instance {i} stopped with status {s.status.name}")
+            # the vertex of the identified basis: the point the adjoint differentiates
+            xs, ys, infos = polish_batch(probs, [s.x for s in sols], [s.row_duals for s in sols],
+                                         tolerance=adjoint_tol)
+            ctx.probs = probs
+            ctx.xs, ctx.ys = xs, ys
+            ctx.polish_info = infos
+            ctx.adjoint_tol = adjoint_tol
+            ctx.device = c.device
+            return torch.from_numpy(np.stack(xs)).to(c.device)
+
+        @staticmethod
+        def backward(ctx, grad_x):
+            g = grad_x.detach().to("cpu", torch.float64).numpy()
+            grads, infos = adjoint_batch(ctx.probs, ctx.xs, ctx.ys, list(g), tolerance=ctx.adjoint_tol)
+            ctx.adjoint_info = infos
+            stack = lambda k: torch.from_numpy(np.stack([d[k] for d in grads])).to(ctx.device)
+            return (stack("c"), stack("row_lower"), stack("row_upper"), stack("col_lower"), stack("col_upper"),
+                    None, None, None)
+
+    def lp_layer(mats: List[SparseMatrix], c, row_lower, row_upper, col_lower, col_upper,
+                 config: Optional[GpuPdhgConfig] = None, adjoint_tol: float = 1e-6):
+        """x* of each LP of the batch (a (batch, n) float64 tensor), differentiable
+        with respect to the bounds (and c, with a zero implicit part)."""
+        cfg = config if config is not None else GpuPdhgConfig(max_iterations=1_000_000, tol_primal=1e-6,
+                                                               tol_dual=1e-6, tol_gap=1e-6)
+        return LPFunction.apply(c, row_lower, row_upper, col_lower, col_upper, list(mats), cfg, adjoint_tol)

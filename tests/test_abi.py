@@ -129,3 +129,37 @@ def test_generators_are_deterministic():
     cols = np.repeat(np.arange(10000), cnt)
     ref = np.bincount(z.A.csc_row_ind(), weights=z.A.csc_values() * x[cols], minlength=5000)
     np.testing.assert_allclose(dense_ax, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_adjoint_host_path_runs_without_a_device():
+    """The adjoint's host part (validation, basis, layout) runs before the
+    device check; without a GPU the call ends with the no-device status."""
+    import sih_pdhg
+    from sih_pdhg.generators import small_random_lp
+
+    p = small_random_lp(60, 150, 4, 2)
+    rng = np.random.default_rng(0)
+    x = np.clip(rng.uniform(0, 5, 150), p.col_lower, p.col_upper)
+    y = rng.standard_normal(60)
+    if sih_pdhg.GpuSolver.is_cuda_available():
+        pytest.skip("a device is present")
+    with pytest.raises(sih_pdhg.SihPdhgError) as e:
+        sih_pdhg.adjoint_batch([p], [x], [y], [np.ones(150)])
+    assert e.value.code == 2
+    with pytest.raises(sih_pdhg.SihPdhgError):
+        sih_pdhg.adjoint_batch([p], [x[:10]], [y], [np.ones(150)])
+
+
+def test_polish_host_path_runs_without_a_device():
+    import sih_pdhg
+    from sih_pdhg.generators import small_random_lp
+
+    p = small_random_lp(60, 150, 4, 2)
+    rng = np.random.default_rng(0)
+    x = np.clip(rng.uniform(0, 5, 150), p.col_lower, p.col_upper)
+    y = rng.standard_normal(60)
+    if sih_pdhg.GpuSolver.is_cuda_available():
+        pytest.skip("a device is present")
+    with pytest.raises(sih_pdhg.SihPdhgError) as e:
+        sih_pdhg.polish_batch([p], [x], [y])
+    assert e.value.code == 2
