@@ -138,8 +138,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_s(Side unk_side, CgVecs V, CgIn
 
 // r -= alpha q (residual side), z += alpha p (unknown side)
 __global__ void __launch_bounds__(kThreads) k_cg_step(Chunks ch, CgVecs V, CgInst* __restrict__ st, int unk_col) {
-    for_each_element(ch, st, [&](bool is_col, const CgInst& S, int k) {
-        const float a = (float)S.alpha;
+    for_each_element(ch, st, [](const CgInst& S) { return (float)S.alpha; }, [&](bool is_col, float a, int k) {
         if (is_col == (unk_col != 0))
             V.z[k] = fmaf(a, V.p[k], V.z[k]);
         else
@@ -149,8 +148,8 @@ __global__ void __launch_bounds__(kThreads) k_cg_step(Chunks ch, CgVecs V, CgIns
 
 // p = s + beta p (unknown side)
 __global__ void __launch_bounds__(kThreads) k_cg_dir(Chunks ch, CgVecs V, CgInst* __restrict__ st, int unk_col) {
-    for_each_element(ch, st, [&](bool is_col, const CgInst& S, int k) {
-        if (is_col == (unk_col != 0)) V.p[k] = fmaf((float)S.beta, V.p[k], V.s[k]);
+    for_each_element(ch, st, [](const CgInst& S) { return (float)S.beta; }, [&](bool is_col, float b, int k) {
+        if (is_col == (unk_col != 0)) V.p[k] = fmaf(b, V.p[k], V.s[k]);
     });
 }
 

@@ -70,19 +70,25 @@ __device__ __forceinline__ void row_dual_term(Acc& acc, float y, float rl, float
 // ---------------------------------------------------------------- step kernels
 // Elementwise part of a step.  Columns: pending float-float average update of
 // x, then x' = clip(x - tau (c + K^T y), l, u).  Rows: pending average update of y.
+// Scalars of an instance for the elementwise passes (computed once per chunk).
+struct StepScalars {
+    int cur, avg, flag;
+    float w, tau;
+};
+
+__device__ __forceinline__ StepScalars step_scalars(const Inst& S) {
+    return StepScalars{S.cur, S.avg_pending, S.restart_flag, (float)S.avg_w, (float)(S.eta / S.omega)};
+}
+
 __global__ void __launch_bounds__(kThreads) k_step_primal(Chunks ch, Vecs V, Inst* __restrict__ st) {
-    for_each_element(ch, st, [&](bool is_col, const Inst& S, int r) {
-        const int cur = S.cur;
-        const bool avg = S.avg_pending;
-        const float w = (float)S.avg_w;
+    for_each_element(ch, st, step_scalars, [&](bool is_col, const StepScalars& S, int r) {
         if (is_col) {
-            const float xj = pick(V.x0, V.x1, cur)[r];
-            if (avg) V.x_acc[r] = ff_axpy(V.x_acc[r], w, xj);
-            const float tau = (float)(S.eta / S.omega);
-            const float v = fmaf(-tau, V.c[r] + pick(V.kty0, V.kty1, cur)[r], xj);
-            pick(V.x0, V.x1, cur ^ 1)[r] = fminf(fmaxf(v, V.l[r]), V.u[r]);
-        } else if (avg) {
-            V.y_acc[r] = ff_axpy(V.y_acc[r], w, pick(V.y0, V.y1, cur)[r]);
+            const float xj = pick(V.x0, V.x1, S.cur)[r];
+            if (S.avg) V.x_acc[r] = ff_axpy(V.x_acc[r], S.w, xj);
+            const float v = fmaf(-S.tau, V.c[r] + pick(V.kty0, V.kty1, S.cur)[r], xj);
+            pick(V.x0, V.x1, S.cur ^ 1)[r] = fminf(fmaxf(v, V.l[r]), V.u[r]);
+        } else if (S.avg) {
+            V.y_acc[r] = ff_axpy(V.y_acc[r], S.w, pick(V.y0, V.y1, S.cur)[r]);
         }
     });
 }
@@ -200,16 +206,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_step_kty(Side cols, Vecs V, Ins
 // Before an evaluation: applies a pending average update and refreshes the
 // FP32 copies x_avg, y_avg that the evaluation gathers.
 __global__ void __launch_bounds__(kThreads) k_flush_avg(Chunks ch, Vecs V, Inst* __restrict__ st) {
-    for_each_element(ch, st, [&](bool is_col, const Inst& S, int r) {
-        const bool avg = S.avg_pending;
-        const float w = (float)S.avg_w;
+    for_each_element(ch, st, step_scalars, [&](bool is_col, const StepScalars& S, int r) {
         if (is_col) {
             float2 a = V.x_acc[r];
-            if (avg) V.x_acc[r] = a = ff_axpy(a, w, pick(V.x0, V.x1, S.cur)[r]);
+            if (S.avg) V.x_acc[r] = a = ff_axpy(a, S.w, pick(V.x0, V.x1, S.cur)[r]);
             V.x_avg[r] = __fadd_rn(a.x, a.y);
         } else {
             float2 a = V.y_acc[r];
-            if (avg) V.y_acc[r] = a = ff_axpy(a, w, pick(V.y0, V.y1, S.cur)[r]);
+            if (S.avg) V.y_acc[r] = a = ff_axpy(a, S.w, pick(V.y0, V.y1, S.cur)[r]);
             V.y_avg[r] = __fadd_rn(a.x, a.y);
         }
     });
@@ -426,8 +430,8 @@ __global__ void __launch_bounds__(kThreads) k_eval_cols(Side cols, Vecs V, Inst*
 // buffers; either restart makes the new current point the last restart point
 // and the start of the next average.
 __global__ void __launch_bounds__(kThreads) k_restart(Chunks ch, Vecs V, Inst* __restrict__ st) {
-    for_each_element(ch, st, [&](bool is_col, const Inst& S, int r) {
-        const int flag = S.restart_flag;
+    for_each_element(ch, st, step_scalars, [&](bool is_col, const StepScalars& S, int r) {
+        const int flag = S.flag;
         if (flag == 0) return;
         if (is_col) {
             float* x = pick(V.x0, V.x1, S.cur);

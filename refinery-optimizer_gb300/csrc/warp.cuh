@@ -344,16 +344,20 @@ __device__ __forceinline__ void spmv_engine(const Side& side, State* st, Epi& ep
 
 // Elementwise pass over every column (is_col) and row of the running
 // instances: blocks take chunks of kChunk consecutive elements of one
-// instance, threads stride through a chunk (coalesced).
-template <class State, class F>
-__device__ __forceinline__ void for_each_element(const Chunks& ch, State* st, F&& f) {
+// instance, threads stride through a chunk (coalesced).  `prep(S)` turns the
+// instance state into the chunk's scalars once (FP64 arithmetic and
+// conversions stay out of the element loop); `f(is_col, scalars, k)` does one
+// element.
+template <class State, class Prep, class F>
+__device__ __forceinline__ void for_each_element(const Chunks& ch, State* st, Prep&& prep, F&& f) {
     const int nact = *ch.nactive;
     for (int c = blockIdx.x; c < nact; c += gridDim.x) {
         const int4 d = ch.chunks[ch.active[c]];  // begin, end, instance, is_col
         const State& S = st[d.z];
         if (S.done) continue;
         const bool is_col = d.w != 0;
-        for (int r = d.x + threadIdx.x; r < d.y; r += blockDim.x) f(is_col, S, r);
+        const auto sc = prep(S);
+        for (int r = d.x + threadIdx.x; r < d.y; r += blockDim.x) f(is_col, sc, r);
     }
 }
 
