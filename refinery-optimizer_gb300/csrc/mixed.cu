@@ -80,7 +80,17 @@ __device__ __forceinline__ StepScalars step_scalars(const Inst& S) {
     return StepScalars{S.cur, S.avg_pending, S.restart_flag, (float)S.avg_w, (float)(S.eta / S.omega)};
 }
 
-__global__ void __launch_bounds__(kThreads) k_step_primal(Chunks ch, Vecs V, Inst* __restrict__ st) {
+__global__ void __launch_bounds__(kThreads) k_step_primal(int B, Chunks ch, Vecs V, Inst* __restrict__ st) {
+    // the step-size schedule factors of this attempt (FP64 pow is slow on this
+    // part; here it overlaps the streaming instead of the SpMV kernel's tail)
+    if (blockIdx.x == 0)  // the first block to start
+        for (int b = threadIdx.x; b < B; b += blockDim.x) {
+            Inst& S = st[b];
+            if (S.done) continue;
+            const double k = (double)(S.attempts + 2);
+            S.pow06 = pow(k, -0.6);
+            S.pow03 = pow(k, -0.3);
+        }
     for_each_element(ch, st, step_scalars, [&](bool is_col, const StepScalars& S, int r) {
         if (is_col) {
             const float xj = pick(V.x0, V.x1, S.cur)[r];
@@ -139,11 +149,11 @@ __device__ void step_controller(Inst& S, double dx2, double inter) {
     const double movement = om * dx2 + S.dy2 / om;
     const double ai = fabs(inter);
     const double eta_bar = ai > 0.0 ? movement / (2.0 * ai) : INFINITY;
-    // PDLP counts iterations from 1: the base (k + 1) is at least 2
-    const double k = (double)(S.attempts + 2);
+    // PDLP counts iterations from 1: the base k = attempts + 2 is at least 2;
+    // k^-0.6 and k^-0.3 were computed by k_step_primal of this step
     const double eta = S.eta;
-    const double grow = (1.0 + pow(k, -0.6)) * eta;
-    const double eta_next = isinf(eta_bar) ? grow : fmin((1.0 - pow(k, -0.3)) * eta_bar, grow);
+    const double grow = (1.0 + S.pow06) * eta;
+    const double eta_next = isinf(eta_bar) ? grow : fmin((1.0 - S.pow03) * eta_bar, grow);
     S.attempts += 1;
     if (!(movement == movement) || !(inter == inter)) {  // NaN: stop as a numerical failure
         S.done = 3;
@@ -1108,7 +1118,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
 int MixedSolver::launch_step(cudaStream_t s) {
     launches_ += 3;
     Inst* st = state_.as<Inst>();
-    k_step_primal<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st);
+    k_step_primal<<<elem_grid_, kThreads, 0, s>>>(B_, chunks_all_, V_, st);
     k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
     k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
     SIHG_LAUNCH_CHECK();
@@ -1296,7 +1306,7 @@ int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
     for (int k = 0; k < 3 && rc == SIH_PDHG_OK; ++k) {
         cudaEventRecord(e0, s);
         for (int i = 0; i < reps; ++i) {
-            if (k == 0) k_step_primal<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st);
+            if (k == 0) k_step_primal<<<elem_grid_, kThreads, 0, s>>>(B_, chunks_all_, V_, st);
             if (k == 1) k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
             if (k == 2) k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
         }

@@ -56,6 +56,7 @@ struct Inst {
     double beta_suff, beta_nec, beta_art, weight_smoothing;
     double kmax, b2, c2;
     double omega_start;  // > 0: initial primal weight of a warm start
+    double pow06, pow03; // (attempts + 2)^-0.6 and ^-0.3 of the current attempt
 };
 
 struct Side {

@@ -288,7 +288,30 @@ __device__ bool task_complete(const Side& side, int ti, int inst, Acc (&q)[Q], u
     const int ib = side.inst_group_begin[inst], ie = side.inst_group_begin[inst + 1];
 #pragma unroll
     for (int i = 0; i < Q; ++i) v[i].reset();
-    for (int k = ib + lane; k < ie; k += 32) load_slot_join<Q>(side.group_part + (size_t)k * kQ, v, max_mask);
+    // U slots per lane in flight at once (the loop is latency-bound: one
+    // instance can have ~1000 groups); the join order stays k, k + 32, ...
+    constexpr int U = Q <= 2 ? 8 : (Q <= 4 ? 4 : 2);
+    for (int k0 = ib + lane; k0 < ie; k0 += 32 * U) {
+        float2 buf[U][Q];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int k = k0 + 32 * u;
+#pragma unroll
+            for (int i = 0; i < Q; ++i)
+                buf[u][i] = k < ie ? __ldcg(side.group_part + (size_t)k * kQ + i) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (k0 + 32 * u >= ie) break;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                Acc b;
+                b.s = buf[u][i].x;
+                b.c = buf[u][i].y;
+                v[i] = acc_join(v[i], b, (max_mask >> i) & 1u);
+            }
+        }
+    }
     warp_reduce_acc<Q>(v, max_mask);
 #pragma unroll
     for (int i = 0; i < Q; ++i) total[i] = (double)v[i].s + (double)v[i].c;
