@@ -66,10 +66,13 @@ PLAIN_ITERS_LOWER_BOUND = {
     "refinery-64": 100000,
 }
 
-# DRAM bytes per launch of the dominant kernel, read from one ncu capture of
-# the same kernel on the same workload (dram__bytes_read.sum + write.sum);
-# profiles/ holds the capture summary.  None until captured.
-NCU_TRAFFIC_PER_LAUNCH = {}
+# DRAM bytes per launch of the dominant kernels, read from one ncu capture of
+# the same kernel on the same workload (dram__bytes_read.sum + write.sum of one
+# launch in `python bench.py --profile-solve 64`; summaries in profiles/).
+NCU_TRAFFIC_PER_LAUNCH = {
+    ("zipf-500kx1m", "k_step_kty"): 119.71e6,
+    ("zipf-500kx1m", "k_step_dual"): 115.53e6,
+}
 
 
 WORKLOADS = ["zipf-500kx1m", "random-2kx5k", "refinery-168p", "refinery-512", "refinery-64"]
