@@ -23,7 +23,8 @@ Workloads (seeded synthetic LPs, FP64 data, generators in sih_pdhg.generators):
                  scenarios on the same GPU (sampled) for the batched-vs-plain ratio
   refinery-64    the first 64 of those scenarios (a shorter batch)
 
-Multi-GPU: replicas (each rank solves its own copy; scaling "weak").
+Multi-GPU: replicas (each rank solves its own copy of a single LP, or its own
+seeded batch of a batch workload; no data-path exchange; scaling "weak").
 --impl reference times the reference's algorithm (plain FP32 PDHG) through its
 CPU port (oracle/pdhg_oracle.c, OpenMP over all host threads) on a bounded
 sample of iterations, scaled by the iterations that algorithm needs to reach
@@ -110,6 +111,8 @@ def parse_args():
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="batch workloads: scenarios timed with the plain algorithm for the sequential estimate")
+    ap.add_argument("--plain-cap", type=int, default=1_000_000,
+                    help="batch workloads: iteration cap of those plain solves")
     ap.add_argument("--profile-solve", type=int, default=0, metavar="STEPS",
                     help="profiling driver: one mixed solve of exactly STEPS steps, kernels launched one by one "
                          "(no CUDA graph), then exit; prints no bench line")
@@ -127,6 +130,25 @@ def run_profile_solve(args) -> None:
     algo = sih_pdhg.ALGO_MIXED if args.profile_algorithm == "mixed" else sih_pdhg.ALGO_PLAIN
     sol = sih_pdhg.GpuSolver.solve_ex(prob, cfg, algorithm=algo, use_graph=0)
     print(f"profile solve: {sol.simplex_iterations} steps, {sol.time_solver_sec * 1e3:.2f} ms device time")
+
+
+def workload_seed(name: str, rank: int) -> int:
+    """Replicas: every rank solves the same single LP (seed 0); for a batch
+    workload each rank solves its own seeded batch of the same size (per-GPU
+    work fixed, no data-path exchange: weak scaling)."""
+    return rank if name.startswith("refinery-") and name != "refinery-168p" else 0
+
+
+def reduce_max(v: float, world: int, device: str) -> float:
+    """Max of a per-rank float over the process group (the timing rule)."""
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def dist_env():
@@ -290,15 +312,9 @@ def run_gb300(args) -> None:
         torch.cuda.synchronize()
 
     def max_over_ranks(v: float) -> float:
-        if world == 1:
-            return v
-        import torch.distributed as dist
+        return reduce_max(v, world, "cuda")
 
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    work = make_workload(args.workload, seed=0)
+    work = make_workload(args.workload, seed=workload_seed(args.workload, rank))
     probs = as_list(work)
     batch = isinstance(work, list)
     tol = args.tol
@@ -376,7 +392,7 @@ def run_gb300(args) -> None:
     if batch:
         line["iterations_per_instance"] = {"min": min(iters), "median": int(statistics.median(iters)),
                                            "max": max(iters)}
-        line["plain_gpu_sequential"] = plain_sequential_sample(probs, tol, args.plain_sample)
+        line["plain_gpu_sequential"] = plain_sequential_sample(probs, tol, args.plain_sample, args.plain_cap)
     # CPU baseline: the FP64 port of the same algorithm on one instance, scaled
     # to the whole job by nonzero-steps
     big = max(range(len(probs)), key=lambda i: probs[i].num_nonzeros()) if not batch else 0
@@ -391,7 +407,7 @@ def run_gb300(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def plain_sequential_sample(probs, tol: float, count: int) -> dict:
+def plain_sequential_sample(probs, tol: float, count: int, cap: int = 1_000_000) -> dict:
     """The reference algorithm (plain FP32 PDHG) on the same GPU, one scenario
     after another: `count` scenarios (evenly spaced through the batch) solved
     with an iteration cap; the estimate for all scenarios scales the sampled
@@ -399,7 +415,6 @@ def plain_sequential_sample(probs, tol: float, count: int) -> dict:
     estimate a lower bound."""
     import sih_pdhg
 
-    cap = 100_000
     pick = sorted(set(int(round(k)) for k in [i * (len(probs) - 1) / max(1, count - 1) for i in range(count)]))
     secs, nnz_s, reached = 0.0, 0, 0
     for i in pick:

@@ -246,7 +246,8 @@ class CglsBatch {
     double tol_ = 1e-6;
     cudaStream_t s_ = nullptr;
     cudaGraphExec_t graph_[2] = {nullptr, nullptr};
-    DevMem csr_ptr_, csc_ptr_, csr_, csc_, sched_, part_, tick_, vec_, state_, done_;
+    DevMem csr_ptr_, csc_ptr_, csr_, csc_, vec_, state_, done_;
+    TaskLayout layout_;
     Side rows_{}, cols_{};
     Chunks ch_{};
     std::vector<float> F_, R_;
@@ -312,9 +313,6 @@ int CglsBatch::setup(const sih_pdhg_problem* problems, int count, const std::vec
     SIHG_CUDA(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
     const int task_nnz =
         (int)std::max(128LL, std::min(2048LL, nnz / std::max(1LL, 3LL * grid_ * (kThreads / 32))));
-    SideSchedule rs, cs;
-    make_schedule(csr_ptr, roff, task_nnz, rs);
-    make_schedule(csc_ptr, coff, task_nnz, cs);
     auto up = [&](DevMem& d, const void* h, size_t bytes) -> int {
         SIHG_TRY(d.alloc(bytes));
         if (bytes) SIHG_CUDA(cudaMemcpyAsync(d.as<void>(), h, bytes, cudaMemcpyHostToDevice, s_));
@@ -324,89 +322,12 @@ int CglsBatch::setup(const sih_pdhg_problem* problems, int count, const std::vec
     SIHG_TRY(up(csc_ptr_, csc_ptr.data(), sizeof(int) * csc_ptr.size()));
     SIHG_TRY(up(csr_, csr.data(), sizeof(Pair) * csr.size()));
     SIHG_TRY(up(csc_, csc.data(), sizeof(Pair) * csc.size()));
-    // schedules + active lists (every task and chunk stays listed; a finished
-    // instance is skipped by its done flag)
-    std::vector<int4> chunks;
-    std::vector<int> ch_begin(count + 1, 0);
-    for (int b = 0; b < count; ++b) {
-        ch_begin[b] = (int)chunks.size();
-        for (int side = 0; side < 2; ++side) {
-            const std::vector<int>& off = side == 0 ? coff : roff;
-            for (int e0 = off[b]; e0 < off[b + 1]; e0 += kChunk)
-                chunks.push_back(make_int4(e0, std::min(off[b + 1], e0 + kChunk), b, side == 0 ? 1 : 0));
-        }
-    }
-    ch_begin[count] = (int)chunks.size();
-    std::vector<char> buf;
-    auto put = [&](const void* src, size_t n) {
-        const size_t at = buf.size();
-        buf.resize(at + ((n + 15) & ~(size_t)15), 0);
-        if (n) std::memcpy(buf.data() + at, src, n);
-        return at;
-    };
-    auto iota_vec = [](size_t n) {
-        std::vector<int> v(n);
-        for (size_t k = 0; k < n; ++k) v[k] = (int)k;
-        return v;
-    };
-    const std::vector<int> act_r = iota_vec(rs.tasks.size()), act_c = iota_vec(cs.tasks.size()),
-                           act_h = iota_vec(chunks.size());
-    const int counts[4] = {(int)rs.tasks.size(), (int)cs.tasks.size(), (int)chunks.size(), 0};
-    struct SideOff {
-        size_t t, h, x, g, gb, ig, it, act;
-    };
-    auto put_side = [&](const SideSchedule& sc, const std::vector<int>& act) {
-        SideOff o2;
-        o2.t = put(sc.tasks.data(), sizeof(Task) * sc.tasks.size());
-        o2.h = put(sc.list_idx.data(), sizeof(int) * sc.list_idx.size());
-        o2.x = put(sc.light_max.data(), sizeof(int) * sc.light_max.size());
-        o2.g = put(sc.task_group.data(), sizeof(int) * sc.task_group.size());
-        o2.gb = put(sc.group_begin.data(), sizeof(int) * sc.group_begin.size());
-        o2.ig = put(sc.inst_group_begin.data(), sizeof(int) * sc.inst_group_begin.size());
-        o2.it = put(sc.inst_task_begin.data(), sizeof(int) * sc.inst_task_begin.size());
-        o2.act = put(act.data(), sizeof(int) * act.size());
-        return o2;
-    };
-    const SideOff orow = put_side(rs, act_r), ocol = put_side(cs, act_c);
-    const size_t o_ch = put(chunks.data(), sizeof(int4) * chunks.size());
-    const size_t o_chb = put(ch_begin.data(), sizeof(int) * ch_begin.size());
-    const size_t o_cha = put(act_h.data(), sizeof(int) * act_h.size());
-    const size_t o_cnt = put(counts, sizeof(counts));
-    SIHG_TRY(up(sched_, buf.data(), buf.size()));
-    const size_t ng_r = rs.group_begin.size() - 1, ng_c = cs.group_begin.size() - 1;
-    const size_t nt_r = std::max<size_t>(1, rs.tasks.size()), nt_c = std::max<size_t>(1, cs.tasks.size());
-    SIHG_TRY(part_.alloc(sizeof(float2) * kQ * (nt_r + nt_c + std::max<size_t>(1, ng_r) + std::max<size_t>(1, ng_c))));
-    const size_t nticket = 2 * ((size_t)count + 2) + ng_r + ng_c;
-    SIHG_TRY(tick_.alloc(sizeof(unsigned) * nticket));
-    SIHG_CUDA(cudaMemsetAsync(tick_.as<void>(), 0, sizeof(unsigned) * nticket, s_));
-    char* D = sched_.as<char>();
-    float2* part = part_.as<float2>();
-    unsigned* tk = tick_.as<unsigned>();
-    int* cnt = (int*)(D + o_cnt);
-    auto mk_side = [&](const SegMatrix& A, const SideOff& o2, int ntasks, float2* tp, float2* gp, unsigned* tick,
-                       int* nact) {
-        return Side{A,
-                    (const Task*)(D + o2.t),
-                    ntasks,
-                    (const int*)(D + o2.h),
-                    (const int*)(D + o2.x),
-                    (const int*)(D + o2.g),
-                    (const int*)(D + o2.gb),
-                    (const int*)(D + o2.ig),
-                    tp,
-                    gp,
-                    tick + count + 2,
-                    tick,
-                    tick + count,
-                    (const int*)(D + o2.it),
-                    (int*)(D + o2.act),
-                    nact};
-    };
-    rows_ = mk_side(SegMatrix{M_, csr_ptr_.as<int>(), csr_.as<int2>()}, orow, (int)rs.tasks.size(), part,
-                    part + kQ * (nt_r + nt_c), tk, cnt);
-    cols_ = mk_side(SegMatrix{N_, csc_ptr_.as<int>(), csc_.as<int2>()}, ocol, (int)cs.tasks.size(), part + kQ * nt_r,
-                    part + kQ * (nt_r + nt_c + std::max<size_t>(1, ng_r)), tk + count + 2 + ng_r, cnt + 1);
-    ch_ = Chunks{(const int4*)(D + o_ch), (int)chunks.size(), (const int*)(D + o_chb), (int*)(D + o_cha), cnt + 2};
+    // every task and chunk stays listed; a finished instance is skipped by its done flag
+    SIHG_TRY(layout_.build(csr_ptr, csc_ptr, roff, coff, SegMatrix{M_, csr_ptr_.as<int>(), csr_.as<int2>()},
+                           SegMatrix{N_, csc_ptr_.as<int>(), csc_.as<int2>()}, task_nnz, true, s_));
+    rows_ = layout_.rows;
+    cols_ = layout_.cols;
+    ch_ = layout_.chunks;
     // vectors: F + 3 column vectors, R + 3 row vectors
     SIHG_TRY(vec_.alloc(sizeof(float) * (4 * (size_t)N_ + 4 * (size_t)M_ + 16)));
     float* v = vec_.as<float>();

@@ -168,6 +168,9 @@ int sih_pdhg_solve_ex(const sih_pdhg_problem* problem, const sih_pdhg_config* co
     SIHG_TRY(validate_config(config));
     HostProblem hp;
     SIHG_TRY(build_host_problem(problem, hp));  // validates sizes, pointers and every index
+    if (opts.verbose)
+        std::fprintf(stderr, "sih_pdhg: host problem %.3f s\n",
+                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
     if (!device_present()) return fail(SIH_PDHG_ERR_NO_DEVICE, "no CUDA device (this engine has no CPU fallback)");
     if (problem->num_rows == 0 || problem->num_cols == 0) {  // gpu_solver.cpp:77-80
         result->status = SIH_STATUS_OPTIMAL;

@@ -464,28 +464,74 @@ __global__ void __launch_bounds__(kThreads) k_restart(Chunks ch, Vecs V, Inst* _
 }
 
 // ---------------------------------------------------------------- setup kernels
-// Per-segment max |a| (mode 0) or sum |a| (mode 1) -> scale 1/sqrt(.) (1 if 0).
-__global__ void k_seg_scale(SegMatrix A, int mode, float* __restrict__ scale) {
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < A.nseg; s += gridDim.x * blockDim.x) {
-        float acc = 0.f;
-        for (int k = A.ptr[s]; k < A.ptr[s + 1]; ++k) {
-            const float a = fabsf(__int_as_float(A.pairs[k].y));
-            acc = mode == 0 ? fmaxf(acc, a) : acc + a;
+// Setup passes over every segment of a side, through its tasks: a light
+// task's lanes take one segment each (segments longer than light_max are
+// skipped), a list task's warp takes its listed segments one by one.  Every
+// segment is visited exactly once, long ones by a whole warp.
+template <class Light, class Long>
+__device__ __forceinline__ void for_each_segment_tasks(const Side& sd, Light&& light, Long&& heavy) {
+    const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int ti = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ti < sd.ntasks; ti += nw) {
+        const Task t = sd.tasks[ti];
+        if (t.flags & kTaskList) {
+            for (int h = t.seg_begin; h < t.seg_end; ++h) heavy(sd.list_idx[h], lane);
+        } else {
+            const int lmax = sd.light_max[t.inst];
+            for (int r = t.seg_begin + lane; r < t.seg_end; r += 32) {
+                const int b = sd.A.ptr[r], e = sd.A.ptr[r + 1];
+                if (e - b <= lmax) light(r, b, e);
+            }
         }
-        scale[s] = acc > 0.f ? 1.0f / sqrtf(acc) : 1.0f;
     }
 }
 
+// Per-segment max |a| (mode 0) or sum |a| (mode 1) -> scale 1/sqrt(.) (1 if 0).
+// Sums keep the entry order (one thread per segment).
+__global__ void k_seg_scale(Side sd, int mode, float* __restrict__ scale) {
+    const SegMatrix A = sd.A;
+    auto fin_scale = [](float acc) { return acc > 0.f ? 1.0f / sqrtf(acc) : 1.0f; };
+    for_each_segment_tasks(
+        sd,
+        [&](int r, int b, int e) {
+            float acc = 0.f;
+            for (int k = b; k < e; ++k) {
+                const float a = fabsf(__int_as_float(A.pairs[k].y));
+                acc = mode == 0 ? fmaxf(acc, a) : acc + a;
+            }
+            scale[r] = fin_scale(acc);
+        },
+        [&](int r, int lane) {
+            const int b = A.ptr[r], e = A.ptr[r + 1];
+            float acc = 0.f;
+            if (mode == 0) {
+                for (int k = b + lane; k < e; k += 32) acc = fmaxf(acc, fabsf(__int_as_float(A.pairs[k].y)));
+                acc = warp_max(acc);
+            } else if (lane == 0) {
+                for (int k = b; k < e; ++k) acc += fabsf(__int_as_float(A.pairs[k].y));
+            }
+            if (lane == 0) scale[r] = fin_scale(acc);
+        });
+}
+
 // a <- a * own[seg] * other[index] for every entry of one side.
-__global__ void k_scale_entries(SegMatrix A, const float* __restrict__ own, const float* __restrict__ other) {
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < A.nseg; s += gridDim.x * blockDim.x) {
-        const float fs = own[s];
-        for (int k = A.ptr[s]; k < A.ptr[s + 1]; ++k) {
-            int2 p = A.pairs[k];
-            p.y = __float_as_int(__int_as_float(p.y) * fs * other[p.x]);
-            const_cast<int2*>(A.pairs)[k] = p;
-        }
-    }
+__global__ void k_scale_entries(Side sd, const float* __restrict__ own, const float* __restrict__ other) {
+    int2* pairs = const_cast<int2*>(sd.A.pairs);
+    auto upd = [&](int k, float fs) {
+        int2 p = pairs[k];
+        p.y = __float_as_int(__int_as_float(p.y) * fs * other[p.x]);
+        pairs[k] = p;
+    };
+    for_each_segment_tasks(
+        sd,
+        [&](int r, int b, int e) {
+            const float fs = own[r];
+            for (int k = b; k < e; ++k) upd(k, fs);
+        },
+        [&](int r, int lane) {
+            const float fs = own[r];
+            for (int k = sd.A.ptr[r] + lane; k < sd.A.ptr[r + 1]; k += 32) upd(k, fs);
+        });
 }
 
 __global__ void k_mul_inplace(int n, float* __restrict__ acc, const float* __restrict__ f) {
@@ -508,7 +554,8 @@ __global__ void k_scale_vectors(int N, int M, float* c, float* l, float* u, cons
 
 // Per-instance statistics of the scaled problem for the initial step size and
 // primal weight: rows give max |a~| and |b~|^2, columns give |c~|^2.  Light
-// tasks cover every segment and nonzero (list tasks contribute nothing).
+// tasks cover every segment (|b~|^2, |c~|^2) and the light segments' entries,
+// list tasks the long segments' entries.
 template <bool ROWS>
 struct StatsEpi {
     Vecs V;
@@ -536,9 +583,20 @@ __device__ void init_stats_side(const Side& sd, const Vecs& V, Inst* st) {
     const int lane = threadIdx.x & 31;
     StatsEpi<ROWS> epi{V, 0.f, Acc{}};
     task_loop<2>(sd, st, epi, 0x1u, [&](const Task& t, const Inst&) {
-        if (t.flags & kTaskList) return;
-        const int k0 = sd.A.ptr[t.seg_begin], k1 = sd.A.ptr[t.seg_end];
-        for (int k = k0 + lane; k < k1; k += 32) epi.amax = fmaxf(epi.amax, fabsf(__int_as_float(sd.A.pairs[k].y)));
+        if (t.flags & kTaskList) {  // max |a| over the listed (long) segments
+            for (int h = t.seg_begin; h < t.seg_end; ++h) {
+                const int r = sd.list_idx[h];
+                for (int k = sd.A.ptr[r] + lane; k < sd.A.ptr[r + 1]; k += 32)
+                    epi.amax = fmaxf(epi.amax, fabsf(__int_as_float(sd.A.pairs[k].y)));
+            }
+            return;
+        }
+        const int lmax = sd.light_max[t.inst];
+        for (int r = t.seg_begin + lane; r < t.seg_end; r += 32) {  // max |a| over the light segments
+            const int b = sd.A.ptr[r], e = sd.A.ptr[r + 1];
+            if (e - b > lmax) continue;
+            for (int k = b; k < e; ++k) epi.amax = fmaxf(epi.amax, fabsf(__int_as_float(sd.A.pairs[k].y)));
+        }
         for (int s = t.seg_begin + lane; s < t.seg_end; s += 32) {
             if (ROWS) {
                 const float lo = V.rl[s], hi = V.ru[s];
@@ -818,99 +876,13 @@ static int upload(DevMem& d, const void* h, size_t bytes, cudaStream_t s) {
 // Tasks, reduction groups, tickets, element chunks and active lists for SpMV
 // tasks of about `task_nnz` nonzeros (rebuilt by the autotuner).
 int MixedSolver::build_schedules(int task_nnz) {
-    cudaStream_t s = stream_;
     task_nnz_ = task_nnz;
-    SideSchedule rs, cs;
-    make_schedule(h_csr_ptr_, row_off_, task_nnz_, rs);
-    make_schedule(h_csc_ptr_, col_off_, task_nnz_, cs);
-    // per side: tickets [B] + counters [2] + group tickets [ngroups], zeroed once;
-    // the kernels leave them zero
-    const size_t ng_r = rs.group_begin.size() - 1, ng_c = cs.group_begin.size() - 1;
-    const size_t nticket = 2 * ((size_t)B_ + 2) + ng_r + ng_c;
-    SIHG_TRY(tickets_.alloc(sizeof(unsigned) * nticket));
-    SIHG_CUDA(cudaMemsetAsync(tickets_.as<void>(), 0, sizeof(unsigned) * nticket, s));
-    auto upload_schedule = [&](const SideSchedule& sc, DevMem& mem, const SegMatrix& A, DevMem& part,
-                               unsigned* tick, Side& side) -> int {
-        const size_t nt = sc.tasks.size(), ng = sc.group_begin.size() - 1;
-        const size_t bytes = sizeof(Task) * nt +
-                             sizeof(int) * (sc.list_idx.size() + sc.light_max.size() + sc.task_group.size() +
-                                            sc.group_begin.size() + sc.inst_group_begin.size() +
-                                            sc.inst_task_begin.size()) + 112;
-        std::vector<char> buf(bytes, 0);
-        size_t off = 0;
-        auto put = [&](const void* src, size_t n) {
-            const size_t at = off;
-            if (n) std::memcpy(buf.data() + off, src, n);
-            off += (n + 15) & ~(size_t)15;
-            return at;
-        };
-        const size_t o_t = put(sc.tasks.data(), sizeof(Task) * nt);
-        const size_t o_h = put(sc.list_idx.data(), sizeof(int) * sc.list_idx.size());
-        const size_t o_x = put(sc.light_max.data(), sizeof(int) * sc.light_max.size());
-        const size_t o_g = put(sc.task_group.data(), sizeof(int) * sc.task_group.size());
-        const size_t o_b = put(sc.group_begin.data(), sizeof(int) * sc.group_begin.size());
-        const size_t o_i = put(sc.inst_group_begin.data(), sizeof(int) * sc.inst_group_begin.size());
-        const size_t o_s = put(sc.inst_task_begin.data(), sizeof(int) * sc.inst_task_begin.size());
-        buf.resize(std::max<size_t>(off, 16));
-        SIHG_TRY(upload(mem, buf.data(), buf.size(), s));
-        SIHG_TRY(part.alloc(sizeof(float2) * kQ * (std::max<size_t>(1, nt) + std::max<size_t>(1, ng))));
-        char* d = mem.as<char>();
-        float2* tp = part.as<float2>();
-        side = Side{A,
-                    (const Task*)(d + o_t),
-                    (int)nt,
-                    (const int*)(d + o_h),
-                    (const int*)(d + o_x),
-                    (const int*)(d + o_g),
-                    (const int*)(d + o_b),
-                    (const int*)(d + o_i),
-                    tp,
-                    tp + (size_t)kQ * std::max<size_t>(1, nt),
-                    tick + B_ + 2,  // group tickets
-                    tick,           // instance tickets
-                    tick + B_,      // counters
-                    (const int*)(d + o_s),
-                    nullptr,
-                    nullptr};
-        return SIH_PDHG_OK;
-    };
-    unsigned* tk = tickets_.as<unsigned>();
-    SIHG_TRY(upload_schedule(rs, row_sched_, SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()}, row_part_, tk,
-                             rows_));
-    SIHG_TRY(upload_schedule(cs, col_sched_, SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, col_part_,
-                             tk + B_ + 2 + ng_r, cols_));
-    {
-        std::vector<int4> ch;
-        std::vector<int> ch_begin(B_ + 1, 0);
-        for (int b = 0; b < B_; ++b) {
-            ch_begin[b] = (int)ch.size();
-            for (int side = 0; side < 2; ++side) {
-                const std::vector<int>& off = side == 0 ? col_off_ : row_off_;
-                for (int e0 = off[b]; e0 < off[b + 1]; e0 += kChunk)
-                    ch.push_back(make_int4(e0, std::min(off[b + 1], e0 + kChunk), b, side == 0 ? 1 : 0));
-            }
-        }
-        ch_begin[B_] = (int)ch.size();
-        const size_t nch = ch.size();
-        // chunk descriptors, then the chunk instance index
-        std::vector<char> buf(sizeof(int4) * std::max<size_t>(1, nch) + sizeof(int) * (B_ + 1), 0);
-        std::memcpy(buf.data(), ch.data(), sizeof(int4) * nch);
-        std::memcpy(buf.data() + sizeof(int4) * std::max<size_t>(1, nch), ch_begin.data(), sizeof(int) * (B_ + 1));
-        SIHG_TRY(upload(chunks_, buf.data(), buf.size(), s));
-        // active lists: rows tasks, cols tasks, chunks; 3 counts; 3 x B offsets
-        const size_t nr = rows_.ntasks, nc = cols_.ntasks;
-        SIHG_TRY(active_.alloc(sizeof(int) * (nr + nc + nch + 3 + 3 * (size_t)B_ + 8)));
-        int* a = active_.as<int>();
-        rows_.active = a;
-        cols_.active = a + nr;
-        int* cnt = a + nr + nc + nch;
-        rows_.nactive = cnt;
-        cols_.nactive = cnt + 1;
-        chunks_all_ = Chunks{chunks_.as<int4>(), (int)nch,
-                             (const int*)(chunks_.as<char>() + sizeof(int4) * std::max<size_t>(1, nch)),
-                             a + nr + nc, cnt + 2};
-    }
-
+    SIHG_TRY(layout_.build(h_csr_ptr_, h_csc_ptr_, row_off_, col_off_,
+                           SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()},
+                           SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, task_nnz_, false, stream_));
+    rows_ = layout_.rows;
+    cols_ = layout_.cols;
+    chunks_all_ = layout_.chunks;
     return SIH_PDHG_OK;
 }
 
@@ -1068,10 +1040,10 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     float* fr = fc + N_;
     const int g = sm_count_ * 8;
     auto scale_pass = [&](int mode) -> int {
-        k_seg_scale<<<g, 256, 0, s>>>(cols_.A, mode, fc);
-        k_seg_scale<<<g, 256, 0, s>>>(rows_.A, mode, fr);
-        k_scale_entries<<<g, 256, 0, s>>>(rows_.A, fr, fc);
-        k_scale_entries<<<g, 256, 0, s>>>(cols_.A, fc, fr);
+        k_seg_scale<<<g, 256, 0, s>>>(cols_, mode, fc);
+        k_seg_scale<<<g, 256, 0, s>>>(rows_, mode, fr);
+        k_scale_entries<<<g, 256, 0, s>>>(rows_, fr, fc);
+        k_scale_entries<<<g, 256, 0, s>>>(cols_, fc, fr);
         k_mul_inplace<<<g, 256, 0, s>>>(N_, C(3), fc);
         k_mul_inplace<<<g, 256, 0, s>>>(M_, R(2), fr);
         SIHG_LAUNCH_CHECK();
@@ -1139,7 +1111,7 @@ int MixedSolver::launch_eval(cudaStream_t s) {
 int MixedSolver::launch_compact(cudaStream_t s) {
     launches_ += 2;
     Inst* st = state_.as<Inst>();
-    int* off = rows_.nactive + 3;  // 3 x B offsets after the three counts
+    int* off = layout_.compaction_offsets();
     k_compact_offsets<<<1, 1024, 0, s>>>(B_, st, rows_.inst_task_begin, cols_.inst_task_begin,
                                          chunks_all_.inst_begin, off, rows_.nactive, rows_.counters,
                                          cols_.counters);
@@ -1409,14 +1381,24 @@ int MixedSolver::autotune() {
 
 int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
                 sih_pdhg_result* r) {
+    using clk = std::chrono::steady_clock;
+    auto secs = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+    const auto t0 = clk::now();
     MixedSolver solver;
     std::vector<const HostProblem*> probs{&hp};
     SIHG_TRY(solver.setup(probs, cfg, opts));
+    cudaStreamSynchronize(solver.stream());
+    const auto t1 = clk::now();
     SIHG_TRY(solver.run());
+    const auto t2 = clk::now();
     std::vector<double> x, y;
     SIHG_TRY(solver.fetch(0, x, y));
+    const auto t3 = clk::now();
     solver.fill_result(0, r);
     pack_solution(hp.src, opts, x, y, r);
+    if (opts.verbose)
+        std::fprintf(stderr, "sih_pdhg mixed: setup %.3f s, run %.3f s (device %.3f s), fetch %.3f s, pack %.3f s\n",
+                     secs(t0, t1), secs(t1, t2), solver.loop_seconds(), secs(t2, t3), secs(t3, clk::now()));
     r->d2h_bytes = 8ull * (hp.n + hp.m);
     r->h2d_bytes = instance_h2d_bytes(hp);
     return SIH_PDHG_OK;

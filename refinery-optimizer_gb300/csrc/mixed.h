@@ -98,6 +98,29 @@ struct SideSchedule {
 // light nonzeros, then list tasks per length class) and their reduction groups.
 void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out);
 
+// Device task layout of a block-diagonal (batched) matrix for the task engine
+// (warp.cuh): per side (rows = CSR for A x, columns = CSC for A^T y) the SpMV
+// tasks, their reduction groups, partial slots, tickets and active list; the
+// element chunks of both sides and their active list (layout.cu).
+class TaskLayout {
+  public:
+    // csr_ptr / csc_ptr: segment pointers of the concatenated matrix (device
+    // order); roff / coff: row / column offsets of the instances.  With
+    // all_active the active lists hold every task and chunk (no compaction
+    // pass needed); otherwise the compaction kernels fill them.
+    int build(const std::vector<int>& csr_ptr, const std::vector<int>& csc_ptr, const std::vector<int>& roff,
+              const std::vector<int>& coff, const SegMatrix& rows_A, const SegMatrix& cols_A, int task_nnz,
+              bool all_active, cudaStream_t s);
+
+    Side rows{}, cols{};
+    Chunks chunks{};
+    // 3 x B ints after the three active counts (scratch of the compaction)
+    int* compaction_offsets() const { return rows.nactive + 3; }
+
+  private:
+    DevMem row_sched_, col_sched_, row_part_, col_part_, tickets_, chunks_, active_;
+};
+
 struct Vecs {
     // column side (length N)
     const float *c, *l, *u, *dcol;
@@ -164,8 +187,9 @@ class MixedSolver {
     std::vector<int> row_off_, col_off_;
     std::vector<int> col_perm_, row_perm_;  // device order -> instance-local original index
     std::vector<int> h_csr_ptr_, h_csc_ptr_;  // segment pointers (device order), for schedule rebuilds
-    DevMem csr_ptr_, csc_ptr_, csr_pairs_, csc_pairs_, row_sched_, col_sched_;
-    DevMem row_part_, col_part_, tickets_, colvec_, rowvec_, state_, done_count_, accvec_, chunks_, active_;
+    DevMem csr_ptr_, csc_ptr_, csr_pairs_, csc_pairs_;
+    DevMem colvec_, rowvec_, state_, done_count_, accvec_;
+    TaskLayout layout_;
     Side rows_{}, cols_{};
     Chunks chunks_all_{};
     int elem_grid_ = 1;

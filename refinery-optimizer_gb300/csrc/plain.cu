@@ -22,6 +22,7 @@
 
 #include "plain.h"
 #include "spmv.cuh"
+#include "warp.cuh"
 
 namespace sihg {
 
@@ -98,6 +99,31 @@ __global__ void __launch_bounds__(256, 8) plain_dual_kernel(SegMatrix A, SpmvPla
     if (st->done) return;
     DualEpi epi{v};
     spmv_run<EXACT>(A, P, v.xbar, epi);
+}
+
+// Fast path of the iteration (exact_arithmetic = 0): the same epilogues on
+// the task engine (warp.cuh: dynamic warp tasks, software-pipelined loads).
+template <class E>
+struct PlainTaskEpi {
+    E e;
+    const float* vec;
+    using Pre = typename E::Pre;
+    __device__ __forceinline__ Pre pre(int k) const { return e.pre(k); }
+    __device__ __forceinline__ void begin(const PlainState&) {}
+    __device__ __forceinline__ const float* gather(int) const { return vec; }
+    __device__ __forceinline__ void apply(int k, const SegDot<1>& d, const Pre& p) { e.apply(k, d.s[0], p); }
+};
+
+__global__ void __launch_bounds__(kThreads, 4) plain_primal_tasks(Side cols, PlainVecs v, PlainState* st) {
+    if (st->done) return;
+    PlainTaskEpi<PrimalEpi> epi{PrimalEpi{v}, v.y};
+    spmv_engine<1, false, 0>(cols, st, epi, 0u);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) plain_dual_tasks(Side rows, PlainVecs v, PlainState* st) {
+    if (st->done) return;
+    PlainTaskEpi<DualEpi> epi{DualEpi{v}, v.xbar};
+    spmv_engine<1, false, 0>(rows, st, epi, 0u);
 }
 
 template <bool EXACT>
@@ -229,6 +255,17 @@ int PlainSolver::setup(const HostProblem& hp, const sih_pdhg_config& cfg, const 
     plan_csr_.heavy_idx = heavy_.as<int>() + heavy_c.size();
     At_ = SegMatrix{n, csc_ptr_.as<int>(), csc_pairs_.as<int2>()};
     A_ = SegMatrix{m, csr_ptr_.as<int>(), csr_pairs_.as<int2>()};
+    if (!exact_ && m > 0 && n > 0) {  // task engine of the fast iteration kernels
+        int occ = 0;
+        SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, plain_primal_tasks, kThreads, 0));
+        task_grid_ = sm_count_ * std::max(1, occ);
+        const long long warps = (long long)task_grid_ * (kThreads / 32);
+        const int task_nnz = opts.tile_nnz > 0
+                                 ? opts.tile_nnz
+                                 : (int)std::max(128LL, std::min(2048LL, (long long)nnz / std::max(1LL, 3 * warps)));
+        SIHG_TRY(layout_.build(hp.csr_ptr, hp.csc_ptr, std::vector<int>{0, m}, std::vector<int>{0, n}, A_, At_,
+                               task_nnz, true, s));
+    }
 
     // step sizes on the device, in the reference's summation order
     if (n > 0) {
@@ -265,8 +302,9 @@ int PlainSolver::launch_iteration(cudaStream_t s) {
         plain_primal_kernel<true><<<plan_csc_.grid(), plan_csc_.threads, 0, s>>>(At_, plan_csc_, vec_, st);
         plain_dual_kernel<true><<<plan_csr_.grid(), plan_csr_.threads, 0, s>>>(A_, plan_csr_, vec_, st);
     } else {
-        plain_primal_kernel<false><<<plan_csc_.grid(), plan_csc_.threads, 0, s>>>(At_, plan_csc_, vec_, st);
-        plain_dual_kernel<false><<<plan_csr_.grid(), plan_csr_.threads, 0, s>>>(A_, plan_csr_, vec_, st);
+        PlainState* sw = state_.as<PlainState>();
+        plain_primal_tasks<<<task_grid_, kThreads, 0, s>>>(layout_.cols, vec_, sw);
+        plain_dual_tasks<<<task_grid_, kThreads, 0, s>>>(layout_.rows, vec_, sw);
     }
     SIHG_LAUNCH_CHECK();
     return SIH_PDHG_OK;
@@ -292,6 +330,11 @@ int PlainSolver::record_block(int iters, cudaGraphExec_t* exec) {
     cudaGraph_t g = nullptr;
     SIHG_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     int rc = SIH_PDHG_OK;
+    if (!exact_ && layout_.rows.counters) {  // the task counters restart with every block
+        cudaError_t e = cudaMemsetAsync(layout_.rows.counters, 0, sizeof(unsigned), stream_);
+        if (e == cudaSuccess) e = cudaMemsetAsync(layout_.cols.counters, 0, sizeof(unsigned), stream_);
+        if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemsetAsync", __FILE__, __LINE__);
+    }
     for (int k = 0; k < iters && rc == SIH_PDHG_OK; ++k) rc = launch_iteration(stream_);
     if (rc == SIH_PDHG_OK) rc = launch_check(stream_);
     cudaError_t e = cudaStreamEndCapture(stream_, &g);
@@ -333,6 +376,10 @@ int PlainSolver::reset_state() {
     st.max_iterations = cfg_.max_iterations;
     host_state_ = st;
     SIHG_CUDA(cudaMemcpyAsync(state_.as<PlainState>(), &host_state_, sizeof(PlainState), cudaMemcpyHostToDevice, s));
+    if (!exact_ && layout_.rows.counters) {
+        SIHG_CUDA(cudaMemsetAsync(layout_.rows.counters, 0, sizeof(unsigned), s));
+        SIHG_CUDA(cudaMemsetAsync(layout_.cols.counters, 0, sizeof(unsigned), s));
+    }
     return SIH_PDHG_OK;
 }
 
@@ -373,6 +420,10 @@ int PlainSolver::iterate() {
                 if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
             } else {
                 const int its = is_tail ? tail : cf;
+                if (!exact_ && layout_.rows.counters) {  // task counters restart with every block
+                    cudaMemsetAsync(layout_.rows.counters, 0, sizeof(unsigned), s);
+                    cudaMemsetAsync(layout_.cols.counters, 0, sizeof(unsigned), s);
+                }
                 for (int k = 0; k < its && rc == SIH_PDHG_OK; ++k) rc = launch_iteration(s);
                 if (rc == SIH_PDHG_OK) rc = launch_check(s);
             }

@@ -5,6 +5,7 @@
 
 #include "common.cuh"
 #include "host.h"
+#include "mixed.h"
 #include "spmv.cuh"
 
 namespace sihg {
@@ -27,6 +28,7 @@ struct PlainState {
     float tol_d;
     int check_frequency;
     int max_iterations;
+    int refine;          // task-engine flag (compensated SpMVs): always 0 here
 };
 
 struct PlainVecs {
@@ -75,6 +77,8 @@ class PlainSolver {
     cudaEvent_t ev_start_ = nullptr, ev_stop_ = nullptr;
     cudaGraphExec_t block_exec_ = nullptr, tail_exec_ = nullptr;
     DevMem csc_ptr_, csr_ptr_, csc_pairs_, csr_pairs_, colvec_, rowvec_, state_, heavy_;
+    TaskLayout layout_;   // task engine of the fast (non-exact) iteration kernels
+    int task_grid_ = 1;
     SegMatrix A_{}, At_{};
     SpmvPlan plan_csr_{}, plan_csc_{};
     PlainVecs vec_{};

@@ -341,11 +341,13 @@ __device__ __forceinline__ void task_loop(const Side& side, State* st, Epi& epi,
         State& S = st[t.inst];
         if (!S.done) {  // uniform over the warp; it only changes after the instance's last task
             body(t, S);
-            Acc q[Q];
-            epi.values(q);
-            double tot[Q];
-            if (task_complete<Q>(side, ti, t.inst, q, max_mask, tot) && lane == 0) epi.finish(S, tot);
-            __syncwarp();
+            if constexpr (Q > 0) {  // Q = 0: no reductions, no tickets
+                Acc q[Q];
+                epi.values(q);
+                double tot[Q];
+                if (task_complete<Q>(side, ti, t.inst, q, max_mask, tot) && lane == 0) epi.finish(S, tot);
+                __syncwarp();
+            }
         }
         pos = __shfl_sync(FULL_MASK, next, 0);
     }

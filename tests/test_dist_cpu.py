@@ -1,0 +1,63 @@
+"""Multi-process paths of bench.py on CPU (gloo, world size 2): the max-over-
+ranks timing reduction, the per-rank workload seeds of the replica layout,
+and the reference arm's launch contract (rank 0 prints one JSON line, the
+other ranks exit 0 without output)."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+from conftest import REPO
+
+torch = pytest.importorskip("torch")
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, out):
+    import torch.distributed as dist
+
+    sys.path.insert(0, REPO)
+    import bench
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        out[rank] = (bench.reduce_max(float(rank + 1) * 0.5, world, "cpu"),
+                     bench.workload_seed("refinery-512", rank), bench.workload_seed("zipf-500kx1m", rank))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_reduce_max_and_seeds_world_size_2():
+    import torch.multiprocessing as mp
+
+    port = _free_port()
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
+    assert out[0][0] == out[1][0] == 1.0
+    assert {out[0][1], out[1][1]} == {0, 1}  # own batch per rank
+    assert out[0][2] == out[1][2] == 0  # the same single LP on every rank
+
+
+def test_reference_arm_under_torchrun_world_size_2():
+    port = _free_port()
+    env = dict(os.environ)
+    env.pop("CUDA_VISIBLE_DEVICES", None)
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(REPO, "bench.py"),
+           "--impl", "reference", "--workload", "random-2kx5k", "--gpus", "2", "--steps", "1", "--warmup", "3"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=REPO, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["e2e"]["h2d_bytes_per_step"] == 0
