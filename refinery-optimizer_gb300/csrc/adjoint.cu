@@ -278,7 +278,7 @@ int CglsBatch::setup(const sih_pdhg_problem* problems, int count, const std::vec
     if ((long long)M_ >= INT32_MAX - 64 || (long long)N_ >= INT32_MAX - 64 || nnz >= INT32_MAX - 64)
         return fail(SIH_PDHG_ERR_UNSUPPORTED, "batch exceeds the 32-bit index layout");
     std::vector<int> csr_ptr((size_t)M_ + 1), csc_ptr((size_t)N_ + 1);
-    std::vector<Pair> csr((size_t)nnz), csc((size_t)nnz);
+    PairVec csr((size_t)nnz), csc((size_t)nnz);
     F_.assign(N_, 0.f);
     R_.assign(M_, 0.f);
     std::vector<long long> koff(count + 1, 0);

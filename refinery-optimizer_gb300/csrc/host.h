@@ -5,6 +5,8 @@
 #include <stdint.h>
 
 #include <string>
+#include <memory>
+#include <utility>
 #include <vector>
 
 #include "sih_pdhg.h"
@@ -18,13 +20,35 @@ struct Pair {
     float val;
 };
 
+// Allocator whose resize leaves new elements default-initialised (no zero
+// fill): the large entry arrays are written right after, by several threads.
+template <class T>
+struct NoInitAllocator : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInitAllocator<U>;
+    };
+    NoInitAllocator() = default;
+    template <class U>
+    NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
+    template <class U>
+    void construct(U* p) noexcept {
+        ::new ((void*)p) U;
+    }
+    template <class U, class... A>
+    void construct(U* p, A&&... a) {
+        ::new ((void*)p) U(std::forward<A>(a)...);
+    }
+};
+using PairVec = std::vector<Pair, NoInitAllocator<Pair>>;
+
 // The engine's host copy of one LP.
 struct HostProblem {
     int m = 0, n = 0, nnz = 0;
     std::vector<int> csc_ptr;   // [n + 1]
-    std::vector<Pair> csc;      // [nnz] row index, value (columns' entries)
+    PairVec csc;                // [nnz] row index, value (columns' entries)
     std::vector<int> csr_ptr;   // [m + 1]
-    std::vector<Pair> csr;      // [nnz] column index, value (rows' entries, columns ascending)
+    PairVec csr;                // [nnz] column index, value (rows' entries, columns ascending)
     std::vector<float> c, l, u; // [n] FP32 casts (objective already multiplied by sense)
     std::vector<float> rl, ru;  // [m]
     const sih_pdhg_problem* src = nullptr; // original FP64 data (not owned)

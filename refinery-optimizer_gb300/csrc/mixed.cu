@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <tuple>
 
@@ -799,14 +800,26 @@ void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off
             out.tasks.push_back(Task{s, e, b, L << 8});
             s = e;
         }
-        // list tasks: longer segments by length class (2 lmax, 4 lmax, ...], lanes doubling per class
-        for (int cls = 1, lo = lmax, L = std::min(32, 2 * L0); lo < (1 << 30); ++cls, lo *= 2, L = std::min(32, 2 * L)) {
-            const int hi = (L == 32) ? (1 << 30) : 2 * lo;
+        // list tasks: longer segments by length class (lmax, 2 lmax], (2 lmax, 4 lmax], ...,
+        // lanes doubling per class; the last class (32 lanes) is open-ended.  One
+        // bucketing pass, segments in index order inside each class.
+        std::vector<std::pair<int, int>> classes;  // (lo, lanes)
+        for (int lo = lmax, L = std::min(32, 2 * L0); lo < (1 << 30); lo *= 2, L = std::min(32, 2 * L)) {
+            classes.push_back({lo, L});
+            if (L == 32) break;
+        }
+        std::vector<std::vector<int>> bucket(classes.size());
+        for (int r = s0; r < s1; ++r) {
+            const int len = ptr[r + 1] - ptr[r];
+            if (len <= lmax) continue;
+            size_t k = 0;
+            while (k + 1 < classes.size() && len > 2 * classes[k].first) ++k;
+            if (len > classes[k].first) bucket[k].push_back(r);
+        }
+        for (size_t kc = 0; kc < classes.size(); ++kc) {
+            const int L = classes[kc].second;
             const int hb = (int)out.list_idx.size();
-            for (int r = s0; r < s1; ++r) {
-                const int len = ptr[r + 1] - ptr[r];
-                if (len > lo && len <= hi) out.list_idx.push_back(r);
-            }
+            out.list_idx.insert(out.list_idx.end(), bucket[kc].begin(), bucket[kc].end());
             int h = hb;
             while (h < (int)out.list_idx.size()) {
                 int e = h;
@@ -899,6 +912,14 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     SIHG_CUDA(cudaEventCreate(&ev_start_));
     SIHG_CUDA(cudaEventCreate(&ev_stop_));
     cudaStream_t s = stream_;
+    auto t_last = std::chrono::steady_clock::now();
+    auto phase = [&](const char* what) {  // options.verbose: host time of each set-up phase
+        if (!opts.verbose) return;
+        cudaStreamSynchronize(s);
+        const auto t = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "sih_pdhg setup: %-18s %.4f s\n", what, std::chrono::duration<double>(t - t_last).count());
+        t_last = t;
+    };
 
     // ---- concatenate the instances (block-diagonal), global indices
     row_off_.assign(B_ + 1, 0);
@@ -915,7 +936,8 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     if ((long long)M_ >= INT32_MAX - 64 || (long long)N_ >= INT32_MAX - 64 || nnz >= INT32_MAX - 64)
         return fail(SIH_PDHG_ERR_UNSUPPORTED, "batch exceeds the 32-bit index layout");
     std::vector<int> csr_ptr((size_t)M_ + 1), csc_ptr((size_t)N_ + 1);
-    std::vector<Pair> csr((size_t)nnz), csc((size_t)nnz);
+    // pair buffers without zero-fill: every entry is written by the parallel copy below
+    std::unique_ptr<Pair[]> csr(new Pair[std::max<long long>(1, nnz)]), csc(new Pair[std::max<long long>(1, nnz)]);
     std::vector<float> c(N_), l(N_), u(N_), rl(M_), ru(M_);
     // Renumbering inside each instance (opts.reorder): columns and rows by
     // descending length.  The entries that long segments share then sit in
@@ -951,7 +973,8 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     });
     csr_ptr[M_] = (int)nnz;
     csc_ptr[N_] = (int)nnz;
-    // entries and vectors, in pieces of at most 32k segments
+    // entries and vectors, in pieces of at most 32k segments and 256k entries
+    // (renumbered sides put the long segments first: count entries, not segments)
     struct Piece {
         int b, cols, k0, k1;
     };
@@ -959,7 +982,15 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     for (int b = 0; b < B_; ++b)
         for (int side = 0; side < 2; ++side) {
             const int cnt = side == 0 ? probs[b]->n : probs[b]->m;
-            for (int k0 = 0; k0 < cnt; k0 += 32768) pieces.push_back(Piece{b, side == 0, k0, std::min(cnt, k0 + 32768)});
+            const int off = side == 0 ? col_off_[b] : row_off_[b];
+            const int* gptr = side == 0 ? csc_ptr.data() : csr_ptr.data();  // renumbered pointers
+            int k0 = 0;
+            while (k0 < cnt) {
+                int k1 = k0 + 1;
+                while (k1 < cnt && k1 - k0 < 32768 && gptr[off + k1] - gptr[off + k0] < (1 << 18)) ++k1;
+                pieces.push_back(Piece{b, side == 0, k0, k1});
+                k0 = k1;
+            }
         }
     // infinite bounds are +-inf (|v| >= 1e20 counts as infinite)
     auto inf_clean = [](double v) -> float {
@@ -993,6 +1024,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
             }
         }
     });
+    phase("concatenate");
     // ---- schedules (tasks and reduction groups per side, element chunks)
     int occ = 0;
     SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_step_dual, kThreads, 0));
@@ -1007,12 +1039,13 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     task_nnz_ = std::max(32, std::min(1 << 20, task_nnz_));
     SIHG_TRY(upload(csr_ptr_, csr_ptr.data(), sizeof(int) * csr_ptr.size(), s));
     SIHG_TRY(upload(csc_ptr_, csc_ptr.data(), sizeof(int) * csc_ptr.size(), s));
-    SIHG_TRY(upload(csr_pairs_, csr.data(), sizeof(Pair) * csr.size(), s));
-    SIHG_TRY(upload(csc_pairs_, csc.data(), sizeof(Pair) * csc.size(), s));
+    SIHG_TRY(upload(csr_pairs_, csr.get(), sizeof(Pair) * (size_t)nnz, s));
+    SIHG_TRY(upload(csc_pairs_, csc.get(), sizeof(Pair) * (size_t)nnz, s));
     h_csr_ptr_ = std::move(csr_ptr);
     h_csc_ptr_ = std::move(csc_ptr);
     SIHG_TRY(build_schedules(task_nnz_));
 
+    phase("schedules+upload");
     // ---- vectors: 11 column vectors, 10 row vectors (layout of Vecs) + float-float averages
     SIHG_TRY(colvec_.alloc(sizeof(float) * (size_t)N_ * 11));
     SIHG_TRY(rowvec_.alloc(sizeof(float) * (size_t)M_ * 10));
@@ -1030,6 +1063,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     SIHG_CUDA(cudaMemcpyAsync(R(0), rl.data(), sizeof(float) * M_, cudaMemcpyHostToDevice, s));
     SIHG_CUDA(cudaMemcpyAsync(R(1), ru.data(), sizeof(float) * M_, cudaMemcpyHostToDevice, s));
 
+    phase("vectors");
     // ---- scaling (Ruiz inf-norm passes, then Pock-Chambolle alpha = 1)
     std::vector<float> ones_c(N_, 1.0f), ones_r(M_, 1.0f);
     SIHG_CUDA(cudaMemcpyAsync(C(3), ones_c.data(), sizeof(float) * N_, cudaMemcpyHostToDevice, s));
@@ -1055,6 +1089,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     SIHG_LAUNCH_CHECK();
     SIHG_CUDA(cudaStreamSynchronize(s));  // tmp is released at scope end
 
+    phase("scaling");
     // ---- per-instance state
     SIHG_TRY(state_.alloc(sizeof(Inst) * B_));
     SIHG_TRY(done_count_.alloc(sizeof(unsigned)));
@@ -1083,6 +1118,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
         S.beta_art = opts.restart_artificial;
         S.weight_smoothing = opts.primal_weight_smoothing;
     }
+    phase("state");
     if (opts.autotune && opts.tile_nnz <= 0) SIHG_TRY(autotune());
     return SIH_PDHG_OK;
 }
