@@ -110,3 +110,17 @@ def test_tile_size_does_not_change_decisions(sih):
     b = sih.solve_gpu_mixed(prob, cfg, tile_nnz=4096)
     assert a.is_optimal() and b.is_optimal()
     assert abs(a.simplex_iterations - b.simplex_iterations) <= 2 * 64
+
+
+def test_renumbering_does_not_change_the_solution(sih):
+    """options.reorder renumbers columns and rows by length on the device only;
+    results come back in the caller's order and agree with the unrenumbered solve."""
+    prob, entry, _ = golden_case("rand_2000x5000_k8_s0")
+    cfg = sih.GpuPdhgConfig(max_iterations=200000, tol_primal=1e-6, tol_dual=1e-6, tol_gap=1e-6)
+    a = sih.solve_gpu_mixed(prob, cfg, reorder=1)
+    b = sih.solve_gpu_mixed(prob, cfg, reorder=0)
+    assert a.is_optimal() and b.is_optimal()
+    ref = entry["highs_objective"]
+    for s in (a, b):
+        assert abs(s.primal_objective - ref) <= 40 * 1e-6 * (1 + abs(ref))
+    np.testing.assert_allclose(a.x, b.x, atol=1e-3 * max(1.0, np.abs(b.x).max()))
