@@ -389,6 +389,8 @@ def run_gb300(args) -> None:
                      "algorithmic_bytes_per_launch": byts[dom], "all_kernels_gbs": all_gbs},
         "plain_reference_iterations_to_tol": plain_its,
     }
+    if not batch and plain_its:
+        line["plain_gpu"] = plain_gpu_time(probs[0], plain_its)
     if batch:
         line["iterations_per_instance"] = {"min": min(iters), "median": int(statistics.median(iters)),
                                            "max": max(iters)}
@@ -405,6 +407,21 @@ def run_gb300(args) -> None:
                          f"(sum over instances of steps x nonzeros)")
     line["cpu_baseline"] = cb
     print(json.dumps(line), flush=True)
+
+
+def plain_gpu_time(prob, its_needed: int, sample_its: int = 2000) -> dict:
+    """The reference algorithm (plain FP32 PDHG) on this GPU: device seconds per
+    iteration from a bounded run (its own termination test disabled by zero
+    tolerances), times the iterations it needs to reach relative KKT <= 1e-4
+    on this LP (PLAIN_ITERS_TO_TOL)."""
+    import sih_pdhg
+
+    cfg = sih_pdhg.GpuPdhgConfig(max_iterations=sample_its, tol_primal=0.0, tol_dual=0.0, tol_gap=0.0)
+    sih_pdhg.solve_gpu_pdhg(prob, cfg)  # warm-up
+    sol = sih_pdhg.solve_gpu_pdhg(prob, cfg)
+    per_it = sol.time_solver_sec / sample_its
+    return {"value": per_it * its_needed, "unit": "s", "per_iteration_s": per_it, "iterations_to_tol": its_needed,
+            "sample": f"{sample_its} iterations of the plain path (sih_pdhg_solve) timed on the device"}
 
 
 def plain_sequential_sample(probs, tol: float, count: int, cap: int = 1_000_000) -> dict:
