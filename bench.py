@@ -391,6 +391,8 @@ def run_gb300(args) -> None:
     }
     if not batch and plain_its:
         line["plain_gpu"] = plain_gpu_time(probs[0], plain_its)
+    if not batch:
+        line["cusparse_yardstick"] = cusparse_yardstick(probs[0])
     if batch:
         line["iterations_per_instance"] = {"min": min(iters), "median": int(statistics.median(iters)),
                                            "max": max(iters)}
@@ -407,6 +409,41 @@ def run_gb300(args) -> None:
                          f"(sum over instances of steps x nonzeros)")
     line["cpu_baseline"] = cb
     print(json.dumps(line), flush=True)
+
+
+def cusparse_yardstick(prob, reps: int = 20) -> dict:
+    """cuSPARSE SpMV (through torch's CSR matrix-vector product) on the same
+    matrix, FP32: A x and A^T y as plain SpMVs, GB/s by the same algorithmic
+    bytes as the engine's (8 nnz + 4 (segments + 1) + 4 gathered + 4 written per
+    segment).  A yardstick only; the engine does not use it."""
+    import numpy as np
+    import torch
+
+    A = prob.A
+    m, n, nnz = prob.num_rows(), prob.num_cols(), prob.num_nonzeros()
+    dev = torch.device("cuda")
+    i32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.int32)).to(dev)
+    f32 = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+    csr = torch.sparse_csr_tensor(i32(A.csr_row_ptr()), i32(A.csr_col_ind()), f32(A.csr_values()), size=(m, n))
+    csc_as_csr = torch.sparse_csr_tensor(i32(A.csc_col_ptr()), i32(A.csc_row_ind()), f32(A.csc_values()), size=(n, m))
+    x = torch.rand(n, 1, device=dev)
+    y = torch.rand(m, 1, device=dev)
+    out = {}
+    for name, mat, vec, segs, gathered in (("A_x", csr, x, m, n), ("AT_y", csc_as_csr, y, n, m)):
+        for _ in range(3):
+            torch.mm(mat, vec)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            torch.mm(mat, vec)
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) * 1e-3 / reps
+        byts = 8.0 * nnz + 4.0 * (segs + 1) + 4.0 * gathered + 4.0 * segs
+        out[name] = {"us": round(sec * 1e6, 1), "gbs": round(byts / sec / 1e9, 1)}
+    out["note"] = "torch CSR matrix-vector product (cuSPARSE), int32 indices, FP32 values; not part of the engine"
+    return out
 
 
 def plain_gpu_time(prob, its_needed: int, sample_its: int = 2000) -> dict:
