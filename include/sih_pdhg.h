@@ -123,13 +123,19 @@ typedef struct sih_pdhg_options {
     int32_t exact_arithmetic;  /* plain: 1 = the reference kernels' arithmetic (one thread per row/column,
                                   entry-order sums, no fused multiply-add); results then equal the CPU
                                   restatement bit for bit.  0 = warp-cooperative SpMV with FMA (default) */
-    int32_t lanes_csr;         /* threads per row of the A x SpMV; 0 = automatic (autotuner or heuristic) */
-    int32_t lanes_csc;         /* threads per column of the A^T y SpMV; 0 = automatic */
+    int32_t lanes_csr;         /* threads per row of the A x SpMV (mixed: lanes per row of the light tasks, a
+                                  power of two <= 32); 0 = automatic (autotuner or heuristic) */
+    int32_t lanes_csc;         /* threads per column of the A^T y SpMV (mixed: as lanes_csr); 0 = automatic */
     int32_t heavy_factor;      /* rows/columns longer than heavy_factor * lanes go to whole warps (16) */
     int32_t tile_nnz;          /* mixed: nonzeros per SpMV task (0 = automatic) */
     int32_t reorder;           /* mixed: 1 = renumber columns and rows by descending length inside each
                                   instance so that the vector entries long segments gather share cache
                                   lines (default); 0 = keep the input order */
+    int32_t staged_kib;        /* mixed, single LP: shared memory (KiB per block) that holds the first entries of
+                                  a gathered vector, so that gathers of the longest segments of the other side
+                                  skip L2; the step SpMVs then run one 1024-thread block per SM.  0 = automatic
+                                  (on where the staged entries carry a large share of the nonzeros), -1 = off */
+    int32_t reserved1;         /* 0 */
 } sih_pdhg_options;
 
 /*

@@ -133,6 +133,7 @@ void sih_pdhg_options_default(sih_pdhg_options* o) {
     o->dual_sign = 0;
     o->use_graph = 1;
     o->reorder = 1;
+    o->staged_kib = 0;
     o->autotune = 0;
     o->verbose = 0;
     o->time_limit_sec = 0.0;

@@ -29,6 +29,10 @@ bool device_present();
 uint64_t instance_h2d_bytes(const HostProblem& p) {
     return 16ull * p.nnz + 4ull * (p.m + 1) + 4ull * (p.n + 1) + 4ull * (3ull * p.n + 2ull * p.m);
 }
+
+// The mixed path also uploads, per segment, its source entry and instance
+// offset (int2) and the inverse of the renumbering (int).
+uint64_t mixed_h2d_bytes(const HostProblem& p) { return instance_h2d_bytes(p) + 12ull * ((uint64_t)p.n + p.m); }
 }  // namespace sihg
 
 extern "C" {
@@ -100,7 +104,7 @@ int sih_pdhg_get_result(sih_pdhg_handle* h, int32_t index, sih_pdhg_result* r) {
     } else {
         SIHG_TRY(solve_plain_packed(*h->plain[index], hp, h->opts, r));
     }
-    r->h2d_bytes = instance_h2d_bytes(hp);
+    r->h2d_bytes = h->mixed ? mixed_h2d_bytes(hp) : instance_h2d_bytes(hp);
     return SIH_PDHG_OK;
 }
 

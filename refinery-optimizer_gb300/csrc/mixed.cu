@@ -41,8 +41,6 @@
 
 namespace sihg {
 
-uint64_t instance_h2d_bytes(const HostProblem& p);
-
 // ---------------------------------------------------------------- helpers
 __device__ __forceinline__ float* pick(float* a, float* b, int sel) { return sel ? b : a; }
 __device__ __forceinline__ bool fin(float v) { return !isinf(v); }
@@ -210,6 +208,34 @@ struct KtyStepEpi {
 
 __global__ void __launch_bounds__(kThreads, 4) k_step_kty(Side cols, Vecs V, Inst* __restrict__ st) {
     KtyStepEpi epi{V};
+    spmv_engine<1, true, 2>(cols, st, epi, 0u);
+}
+
+// Staged variants of the two step SpMVs (single LP): one block of
+// kStagedThreads per SM copies the first `staged` entries (a multiple of 4)
+// of the gathered vector to shared memory, then runs the same tasks with
+// gathers below `staged` served from the copy.  Instance 0's `cur` does not
+// change before the last task of the launch (the controller flips it after).
+struct DualStepEpiStaged : DualStepEpi {
+    static constexpr bool kStaged = true;
+    int staged;
+};
+struct KtyStepEpiStaged : KtyStepEpi {
+    static constexpr bool kStaged = true;
+    int staged;
+};
+
+__global__ void __launch_bounds__(kStagedThreads, 1)
+    k_step_dual_staged(Side rows, Vecs V, Inst* __restrict__ st, int staged) {
+    stage_prefix(pick(V.x0, V.x1, st[0].cur ^ 1), staged);
+    DualStepEpiStaged epi{{V}, staged};
+    spmv_engine<1, true, 1>(rows, st, epi, 0u);
+}
+
+__global__ void __launch_bounds__(kStagedThreads, 1)
+    k_step_kty_staged(Side cols, Vecs V, Inst* __restrict__ st, int staged) {
+    stage_prefix(pick(V.y0, V.y1, st[0].cur ^ 1), staged);
+    KtyStepEpiStaged epi{{V}, staged};
     spmv_engine<1, true, 2>(cols, st, epi, 0u);
 }
 
@@ -583,7 +609,7 @@ template <bool ROWS>
 __device__ void init_stats_side(const Side& sd, const Vecs& V, Inst* st) {
     const int lane = threadIdx.x & 31;
     StatsEpi<ROWS> epi{V, 0.f, Acc{}};
-    task_loop<2>(sd, st, epi, 0x1u, [&](const Task& t, const Inst&) {
+    task_loop<2>(sd, st, epi, 0x1u, [](const Inst&, int) {}, [&](const Task& t, const Inst&) {
         if (t.flags & kTaskList) {  // max |a| over the listed (long) segments
             for (int h = t.seg_begin; h < t.seg_end; ++h) {
                 const int r = sd.list_idx[h];
@@ -770,7 +796,9 @@ static int pow2_floor(int v) {
     return p;
 }
 
-void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out) {
+void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out,
+                   int light_lanes) {
+    if (light_lanes > 0) light_lanes = std::min(32, pow2_floor(light_lanes));
     const int B = (int)inst_off.size() - 1;
     out = SideSchedule{};
     out.light_max.assign(B, 0);
@@ -796,7 +824,8 @@ void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off
                 ++e;
             }
             const int nl = std::max(1, e - s);
-            const int L = std::max(1, std::min(32, pow2_floor(std::max(1, (int)(acc / nl) / kBatch))));
+            const int L = light_lanes > 0 ? light_lanes
+                                          : std::max(1, std::min(32, pow2_floor(std::max(1, (int)(acc / nl) / kBatch))));
             out.tasks.push_back(Task{s, e, b, L << 8});
             s = e;
         }
@@ -865,6 +894,24 @@ MixedSolver::~MixedSolver() {
     if (stream_) cudaStreamDestroy(stream_);
 }
 
+// Renumbered pairs of one side: segment s (new order) takes the entries of
+// its source segment (src[s].x = first source entry, same length) with the
+// other side's indices mapped through inv (src[s].y = that side's instance
+// offset).  One warp per segment, lanes over its entries.
+__global__ void k_renumber_pairs(int nseg, const int* __restrict__ ptr, const int2* __restrict__ src,
+                                 const int2* __restrict__ in, const int* __restrict__ inv, int2* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int sg = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); sg < nseg; sg += nw) {
+        const int b = ptr[sg], len = ptr[sg + 1] - b;
+        const int2 sc = src[sg];
+        for (int k = lane; k < len; k += 32) {
+            const int2 p = in[sc.x + k];
+            out[b + k] = make_int2(inv[sc.y + p.x], p.y);
+        }
+    }
+}
+
 // Stable order of `cnt` segments by descending length (counting sort); the
 // identity without `reorder`.
 static void order_by_length(const int* ptr, int cnt, bool reorder, int* perm) {
@@ -892,7 +939,8 @@ int MixedSolver::build_schedules(int task_nnz) {
     task_nnz_ = task_nnz;
     SIHG_TRY(layout_.build(h_csr_ptr_, h_csc_ptr_, row_off_, col_off_,
                            SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()},
-                           SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, task_nnz_, false, stream_));
+                           SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, task_nnz_, false, stream_,
+                           opts_.lanes_csr, opts_.lanes_csc));
     rows_ = layout_.rows;
     cols_ = layout_.cols;
     chunks_all_ = layout_.chunks;
@@ -936,17 +984,14 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     if ((long long)M_ >= INT32_MAX - 64 || (long long)N_ >= INT32_MAX - 64 || nnz >= INT32_MAX - 64)
         return fail(SIH_PDHG_ERR_UNSUPPORTED, "batch exceeds the 32-bit index layout");
     std::vector<int> csr_ptr((size_t)M_ + 1), csc_ptr((size_t)N_ + 1);
-    // pair buffers without zero-fill: every entry is written by the parallel copy below
-    std::unique_ptr<Pair[]> csr(new Pair[std::max<long long>(1, nnz)]), csc(new Pair[std::max<long long>(1, nnz)]);
     std::vector<float> c(N_), l(N_), u(N_), rl(M_), ru(M_);
     // Renumbering inside each instance (opts.reorder): columns and rows by
     // descending length.  The entries that long segments share then sit in
     // few cache lines of the gathered vectors (for Zipf-like column lengths
     // most of A x's gathers hit an L1-sized prefix of x).  perm: new -> old,
-    // inv: old -> new, both local to the instance.
+    // local to the instance.
     col_perm_.assign(N_, 0);
     row_perm_.assign(M_, 0);
-    std::vector<int> col_inv(N_), row_inv(M_);
     std::vector<long long> k_off(B_ + 1, 0);
     for (int b = 0; b < B_; ++b) k_off[b + 1] = k_off[b] + probs[b]->nnz;
     const bool reorder = opts.reorder != 0;
@@ -959,9 +1004,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
             const int cnt = cols ? p.n : p.m;
             const int off = cols ? col_off_[b] : row_off_[b];
             int* perm = (cols ? col_perm_.data() : row_perm_.data()) + off;
-            int* inv = (cols ? col_inv.data() : row_inv.data()) + off;
             order_by_length(ptr.data(), cnt, reorder, perm);
-            for (int k = 0; k < cnt; ++k) inv[perm[k]] = k;
             // pointers of the renumbered segments
             int* dst = (cols ? csc_ptr.data() : csr_ptr.data()) + off;
             long long acc = k_off[b];
@@ -973,8 +1016,13 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     });
     csr_ptr[M_] = (int)nnz;
     csc_ptr[N_] = (int)nnz;
-    // entries and vectors, in pieces of at most 32k segments and 256k entries
-    // (renumbered sides put the long segments first: count entries, not segments)
+    // Per renumbered segment (columns, then rows): its first entry in the
+    // pairs as uploaded (each instance's CSC / CSR in its original order) and
+    // the other side's instance offset; inv: global original index -> global
+    // new index (columns, then rows).  The device writes the renumbered pairs
+    // (k_renumber_pairs), so the host work stays O(rows + columns).
+    std::vector<int2> seg_src((size_t)N_ + M_);
+    std::vector<int> inv((size_t)N_ + M_);
     struct Piece {
         int b, cols, k0, k1;
     };
@@ -982,15 +1030,7 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     for (int b = 0; b < B_; ++b)
         for (int side = 0; side < 2; ++side) {
             const int cnt = side == 0 ? probs[b]->n : probs[b]->m;
-            const int off = side == 0 ? col_off_[b] : row_off_[b];
-            const int* gptr = side == 0 ? csc_ptr.data() : csr_ptr.data();  // renumbered pointers
-            int k0 = 0;
-            while (k0 < cnt) {
-                int k1 = k0 + 1;
-                while (k1 < cnt && k1 - k0 < 32768 && gptr[off + k1] - gptr[off + k0] < (1 << 18)) ++k1;
-                pieces.push_back(Piece{b, side == 0, k0, k1});
-                k0 = k1;
-            }
+            for (int k0 = 0; k0 < cnt; k0 += 32768) pieces.push_back(Piece{b, side == 0, k0, std::min(cnt, k0 + 32768)});
         }
     // infinite bounds are +-inf (|v| >= 1e20 counts as infinite)
     auto inf_clean = [](double v) -> float {
@@ -1002,12 +1042,12 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
             const Piece& pc = pieces[q];
             const HostProblem& p = *probs[pc.b];
             const int ro = row_off_[pc.b], co = col_off_[pc.b];
+            const int kb = (int)k_off[pc.b];
             if (pc.cols) {
                 for (int jn = pc.k0; jn < pc.k1; ++jn) {
                     const int j = col_perm_[co + jn];
-                    int at = csc_ptr[co + jn];
-                    for (int k = p.csc_ptr[j]; k < p.csc_ptr[j + 1]; ++k, ++at)
-                        csc[at] = Pair{row_inv[ro + p.csc[k].idx] + ro, p.csc[k].val};
+                    inv[co + j] = co + jn;
+                    seg_src[co + jn] = make_int2(kb + p.csc_ptr[j], ro);
                     c[co + jn] = p.c[j];
                     l[co + jn] = inf_clean(p.src->col_lower[j]);
                     u[co + jn] = inf_clean(p.src->col_upper[j]);
@@ -1015,16 +1055,15 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
             } else {
                 for (int in = pc.k0; in < pc.k1; ++in) {
                     const int i = row_perm_[ro + in];
-                    int at = csr_ptr[ro + in];
-                    for (int k = p.csr_ptr[i]; k < p.csr_ptr[i + 1]; ++k, ++at)
-                        csr[at] = Pair{col_inv[co + p.csr[k].idx] + co, p.csr[k].val};
+                    inv[N_ + ro + i] = ro + in;
+                    seg_src[N_ + ro + in] = make_int2(kb + p.csr_ptr[i], co);
                     rl[ro + in] = inf_clean(p.src->row_lower[i]);
                     ru[ro + in] = inf_clean(p.src->row_upper[i]);
                 }
             }
         }
     });
-    phase("concatenate");
+    phase("renumber");
     // ---- schedules (tasks and reduction groups per side, element chunks)
     int occ = 0;
     SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_step_dual, kThreads, 0));
@@ -1039,11 +1078,37 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     task_nnz_ = std::max(32, std::min(1 << 20, task_nnz_));
     SIHG_TRY(upload(csr_ptr_, csr_ptr.data(), sizeof(int) * csr_ptr.size(), s));
     SIHG_TRY(upload(csc_ptr_, csc_ptr.data(), sizeof(int) * csc_ptr.size(), s));
-    SIHG_TRY(upload(csr_pairs_, csr.get(), sizeof(Pair) * (size_t)nnz, s));
-    SIHG_TRY(upload(csc_pairs_, csc.get(), sizeof(Pair) * (size_t)nnz, s));
+    {
+        // each instance's pairs as they are, then the renumbered sides
+        DevMem src, segs, invd;
+        const size_t nz = (size_t)std::max<long long>(1, nnz);
+        SIHG_TRY(src.alloc(sizeof(Pair) * 2 * nz));
+        Pair* s_csc = src.as<Pair>();
+        Pair* s_csr = s_csc + nz;
+        for (int b = 0; b < B_; ++b) {
+            const size_t nb = (size_t)probs[b]->nnz;
+            if (nb == 0) continue;
+            SIHG_CUDA(cudaMemcpyAsync(s_csc + k_off[b], probs[b]->csc.data(), sizeof(Pair) * nb,
+                                      cudaMemcpyHostToDevice, s));
+            SIHG_CUDA(cudaMemcpyAsync(s_csr + k_off[b], probs[b]->csr.data(), sizeof(Pair) * nb,
+                                      cudaMemcpyHostToDevice, s));
+        }
+        SIHG_TRY(upload(segs, seg_src.data(), sizeof(int2) * seg_src.size(), s));
+        SIHG_TRY(upload(invd, inv.data(), sizeof(int) * inv.size(), s));
+        SIHG_TRY(csc_pairs_.alloc(sizeof(Pair) * nz));
+        SIHG_TRY(csr_pairs_.alloc(sizeof(Pair) * nz));
+        const int g = sm_count_ * 8;
+        k_renumber_pairs<<<g, 256, 0, s>>>(N_, csc_ptr_.as<int>(), segs.as<int2>(), (const int2*)s_csc,
+                                           invd.as<int>() + N_, csc_pairs_.as<int2>());
+        k_renumber_pairs<<<g, 256, 0, s>>>(M_, csr_ptr_.as<int>(), segs.as<int2>() + N_, (const int2*)s_csr,
+                                           invd.as<int>(), csr_pairs_.as<int2>());
+        SIHG_LAUNCH_CHECK();
+        SIHG_CUDA(cudaStreamSynchronize(s));  // the staging buffers are released at scope end
+    }
     h_csr_ptr_ = std::move(csr_ptr);
     h_csc_ptr_ = std::move(csc_ptr);
     SIHG_TRY(build_schedules(task_nnz_));
+    SIHG_TRY(choose_staging());
 
     phase("schedules+upload");
     // ---- vectors: 11 column vectors, 10 row vectors (layout of Vecs) + float-float averages
@@ -1127,9 +1192,70 @@ int MixedSolver::launch_step(cudaStream_t s) {
     launches_ += 3;
     Inst* st = state_.as<Inst>();
     k_step_primal<<<elem_grid_, kThreads, 0, s>>>(B_, chunks_all_, V_, st);
-    k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
-    k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
+    launch_step_spmvs(s, 1);
+    launch_step_spmvs(s, 2);
     SIHG_LAUNCH_CHECK();
+    return SIH_PDHG_OK;
+}
+
+// One of the step SpMVs (which = 1: K x' with the dual update, 2: K^T y' with
+// the step-size controller), staged when choose_staging picked a prefix.
+void MixedSolver::launch_step_spmvs(cudaStream_t s, int which) {
+    Inst* st = state_.as<Inst>();
+    if (which == 1) {
+        if (stage_x_ > 0)
+            k_step_dual_staged<<<sm_count_, kStagedThreads, sizeof(float) * stage_x_, s>>>(rows_, V_, st, stage_x_);
+        else
+            k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
+    } else {
+        if (stage_y_ > 0)
+            k_step_kty_staged<<<sm_count_, kStagedThreads, sizeof(float) * stage_y_, s>>>(cols_, V_, st, stage_y_);
+        else
+            k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
+    }
+}
+
+// Staged gathers (single LP): the first entries of the gathered vector that
+// fit in options.staged_kib of shared memory (automatic: the block opt-in
+// limit, at most 128 KiB) are staged on a side when, after the renumbering by
+// length, their segments on the other side hold at least kStagedShare of the
+// nonzeros; the staged kernels run one block per SM.
+int MixedSolver::choose_staging() {
+    constexpr double kStagedShare = 0.5;
+    stage_x_ = stage_y_ = 0;
+    if (B_ != 1 || opts_.staged_kib < 0 || nnz_ == 0) return SIH_PDHG_OK;
+    int dev = 0, optin = 0;
+    SIHG_CUDA(cudaGetDevice(&dev));
+    SIHG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    size_t bytes = std::min<size_t>((size_t)optin, 128u * 1024u);
+    if (opts_.staged_kib > 0) {
+        bytes = (size_t)opts_.staged_kib * 1024u;
+        if (bytes > (size_t)optin)
+            return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "options.staged_kib exceeds the shared memory of a block");
+    }
+    const int cap = (int)(bytes / sizeof(float));
+    // entries [0, P) of the vector, P a multiple of 4; share of the nonzeros they carry
+    auto pick_prefix = [&](const std::vector<int>& ptr, int cnt) -> int {
+        const int P = std::min(cap, cnt) & ~3;
+        if (P <= 0) return 0;
+        const double share = (double)(ptr[P] - ptr[0]) / (double)nnz_;
+        return (opts_.staged_kib > 0 || share >= kStagedShare) ? P : 0;
+    };
+    stage_x_ = pick_prefix(h_csc_ptr_, N_);  // K x' gathers x' by column
+    stage_y_ = pick_prefix(h_csr_ptr_, M_);  // K^T y' gathers y' by row
+    auto enable = [&](const void* fn, int P, int& out) -> int {
+        if (P == 0) return SIH_PDHG_OK;
+        const int smem = (int)(sizeof(float) * P);
+        SIHG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        int occ = 0;
+        SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kStagedThreads, smem));
+        if (occ < 1) out = 0;
+        return SIH_PDHG_OK;
+    };
+    SIHG_TRY(enable((const void*)k_step_dual_staged, stage_x_, stage_x_));
+    SIHG_TRY(enable((const void*)k_step_kty_staged, stage_y_, stage_y_));
+    if (opts_.verbose)
+        std::fprintf(stderr, "sih_pdhg setup: staged gathers: %d entries of x, %d of y\n", stage_x_, stage_y_);
     return SIH_PDHG_OK;
 }
 
@@ -1315,8 +1441,7 @@ int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
         cudaEventRecord(e0, s);
         for (int i = 0; i < reps; ++i) {
             if (k == 0) k_step_primal<<<elem_grid_, kThreads, 0, s>>>(B_, chunks_all_, V_, st);
-            if (k == 1) k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
-            if (k == 2) k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
+            if (k > 0) launch_step_spmvs(s, k);
         }
         cudaEventRecord(e1, s);
         cudaError_t e = cudaEventSynchronize(e1);
@@ -1436,7 +1561,7 @@ int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdh
         std::fprintf(stderr, "sih_pdhg mixed: setup %.3f s, run %.3f s (device %.3f s), fetch %.3f s, pack %.3f s\n",
                      secs(t0, t1), secs(t1, t2), solver.loop_seconds(), secs(t2, t3), secs(t3, clk::now()));
     r->d2h_bytes = 8ull * (hp.n + hp.m);
-    r->h2d_bytes = instance_h2d_bytes(hp);
+    r->h2d_bytes = mixed_h2d_bytes(hp);
     return SIH_PDHG_OK;
 }
 

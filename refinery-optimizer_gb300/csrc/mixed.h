@@ -13,6 +13,7 @@ namespace sihg {
 
 constexpr int kQ = 12;         // reduction slots per task / group
 constexpr int kThreads = 256;  // threads per block of every task kernel
+constexpr int kStagedThreads = 1024;  // threads per block of the staged step kernels (one block per SM)
 constexpr int kGroup = 32;     // tasks per reduction group (one per lane of the reducing warp)
 constexpr int kChunk = 2048;   // elements per chunk of the elementwise passes
 
@@ -96,7 +97,10 @@ struct SideSchedule {
 
 // Host: tasks of every instance of one side (light tasks of at most task_nnz
 // light nonzeros, then list tasks per length class) and their reduction groups.
-void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out);
+// light_lanes > 0 fixes the lanes per segment of the light tasks (a power of
+// two <= 32); 0 picks them from the task's mean segment length.
+void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out,
+                   int light_lanes = 0);
 
 // Device task layout of a block-diagonal (batched) matrix for the task engine
 // (warp.cuh): per side (rows = CSR for A x, columns = CSC for A^T y) the SpMV
@@ -110,7 +114,7 @@ class TaskLayout {
     // pass needed); otherwise the compaction kernels fill them.
     int build(const std::vector<int>& csr_ptr, const std::vector<int>& csc_ptr, const std::vector<int>& roff,
               const std::vector<int>& coff, const SegMatrix& rows_A, const SegMatrix& cols_A, int task_nnz,
-              bool all_active, cudaStream_t s);
+              bool all_active, cudaStream_t s, int row_lanes = 0, int col_lanes = 0);
 
     Side rows{}, cols{};
     Chunks chunks{};
@@ -168,6 +172,8 @@ class MixedSolver {
     int autotune();
     int launch_compact(cudaStream_t s);
     int record_graph();
+    int choose_staging();
+    void launch_step_spmvs(cudaStream_t s, int which);
 
     std::vector<const HostProblem*> probs_;
     sih_pdhg_config cfg_{};
@@ -193,6 +199,9 @@ class MixedSolver {
     Side rows_{}, cols_{};
     Chunks chunks_all_{};
     int elem_grid_ = 1;
+    // staged gathers (single LP): entries of x (for K x) and of y (for K^T y)
+    // copied to shared memory by every block of the step kernels; 0 = off
+    int stage_x_ = 0, stage_y_ = 0;
     Vecs V_{};
     std::vector<Inst> host_inst_;
     std::vector<std::vector<float>> start_x_, start_y_;  // warm starts (device order, unscaled)
@@ -201,6 +210,8 @@ class MixedSolver {
 int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
                 sih_pdhg_result* r);
 
+// H2D bytes of one instance on the mixed path (problem, vectors, renumbering maps).
+uint64_t mixed_h2d_bytes(const HostProblem& p);
 void pack_solution(const sih_pdhg_problem* p, const sih_pdhg_options& opts, const std::vector<double>& x,
                    const std::vector<double>& y, sih_pdhg_result* r);
 

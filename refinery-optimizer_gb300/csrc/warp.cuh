@@ -55,6 +55,45 @@ struct SegDot {
     __device__ __forceinline__ float f(int v) const { return __fadd_rn(s[v], e[v]); }
 };
 
+// Staged gathers.  An epilogue with `kStaged = true` and a member `staged`
+// (an entry count) works in a kernel whose blocks first copied entries
+// [0, staged) of the gathered vector to the start of dynamic shared memory
+// (stage_prefix): gathers below `staged` read that copy.  With both sides
+// renumbered by descending length the prefix holds the longest segments of
+// the other side, so on skewed matrices (Zipf-like column lengths) most
+// gathers of K x hit the copy instead of going to L2.
+template <class Epi, class = void>
+struct Staged {
+    static constexpr bool value = false;
+};
+template <class Epi>
+struct Staged<Epi, decltype(void(Epi::kStaged))> {
+    static constexpr bool value = Epi::kStaged;
+};
+
+template <class Epi>
+__device__ __forceinline__ float gather_one(const Epi& epi, const float* __restrict__ vec, int idx) {
+    if constexpr (Staged<Epi>::value) {
+        extern __shared__ float stage_vec[];
+        if (idx < epi.staged) return stage_vec[idx];
+    }
+    return ld_vec(vec + idx);
+}
+
+// Copies v[0, n) to the start of dynamic shared memory (all threads of the
+// block, then a block barrier).  n is a multiple of 4.
+__device__ __forceinline__ void stage_prefix(const float* __restrict__ v, int n) {
+    extern __shared__ float stage_vec[];
+    if ((reinterpret_cast<uintptr_t>(v) & 15) == 0) {
+        const float4* __restrict__ v4 = reinterpret_cast<const float4*>(v);
+        float4* s4 = reinterpret_cast<float4*>(stage_vec);
+        for (int k = threadIdx.x; k < (n >> 2); k += blockDim.x) s4[k] = __ldcg(v4 + k);
+    } else {
+        for (int k = threadIdx.x; k < n; k += blockDim.x) stage_vec[k] = __ldcg(v + k);
+    }
+    __syncthreads();
+}
+
 // Loads one batch of a lane's pairs (entries k, k + L, ..., k + (kBatch-1) L
 // below `end`); the rest are zero.
 __device__ __forceinline__ void load_batch(bool on, const int2* __restrict__ pairs, int k, int end, int L,
@@ -90,7 +129,7 @@ __device__ __forceinline__ void seg_dots(const int2* __restrict__ pairs, int beg
                 const float* __restrict__ vec = epi.gather(v);
                 float g[kBatch];
 #pragma unroll
-                for (int u = 0; u < kBatch; ++u) g[u] = (k + u * L < end) ? ld_vec(vec + p[u].x) : 0.f;
+                for (int u = 0; u < kBatch; ++u) g[u] = (k + u * L < end) ? gather_one(epi, vec, p[u].x) : 0.f;
 #pragma unroll
                 for (int u = 0; u < kBatch; ++u) {
                     if (COMP) {
@@ -336,7 +375,7 @@ __device__ __forceinline__ void task_loop(const Side& side, State* st, Epi& epi,
         // after each evaluation zeroes the counter.
         int next = 0;
         if (lane == 0) next = (int)(atomicAdd(&side.counters[0], 1u) % (unsigned)nact) + nw;
-        const int ti = side.active[pos];
+        const int ti = nact == side.ntasks ? pos : side.active[pos];
         const Task t = side.tasks[ti];
         State& S = st[t.inst];
         if (!S.done) {  // uniform over the warp; it only changes after the instance's last task
@@ -351,6 +390,12 @@ __device__ __forceinline__ void task_loop(const Side& side, State* st, Epi& epi,
         }
         pos = __shfl_sync(FULL_MASK, next, 0);
     }
+}
+
+template <int Q, class Epi, class State, class Prep, class Body>
+__device__ __forceinline__ void task_loop(const Side& side, State* st, Epi& epi, unsigned max_mask, Prep&&,
+                                          Body&& body) {
+    task_loop<Q>(side, st, epi, max_mask, body);
 }
 
 // SpMV engine: the tasks of the side with the epilogue Epi.  With ALLOW_COMP

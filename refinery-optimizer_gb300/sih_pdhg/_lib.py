@@ -46,7 +46,8 @@ class COptions(C.Structure):
                 ("restart_necessary", C.c_double), ("restart_artificial", C.c_double),
                 ("primal_weight_smoothing", C.c_double), ("exact_arithmetic", C.c_int32),
                 ("lanes_csr", C.c_int32), ("lanes_csc", C.c_int32), ("heavy_factor", C.c_int32),
-                ("tile_nnz", C.c_int32), ("reorder", C.c_int32)]
+                ("tile_nnz", C.c_int32), ("reorder", C.c_int32), ("staged_kib", C.c_int32),
+                ("reserved1", C.c_int32)]
 
 
 class CAdjointOptions(C.Structure):
