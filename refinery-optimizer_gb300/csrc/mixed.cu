@@ -80,26 +80,83 @@ __device__ __forceinline__ StepScalars step_scalars(const Inst& S) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_step_primal(int B, Chunks ch, Vecs V, Inst* __restrict__ st) {
-    // the step-size schedule factors of this attempt (FP64 pow is slow on this
-    // part; here it overlaps the streaming instead of the SpMV kernel's tail)
-    if (blockIdx.x == 0)  // the first block to start
-        for (int b = threadIdx.x; b < B; b += blockDim.x) {
-            Inst& S = st[b];
-            if (S.done) continue;
-            const double k = (double)(S.attempts + 2);
-            S.pow06 = pow(k, -0.6);
-            S.pow03 = pow(k, -0.3);
-        }
-    for_each_element(ch, st, step_scalars, [&](bool is_col, const StepScalars& S, int r) {
-        if (is_col) {
-            const float xj = pick(V.x0, V.x1, S.cur)[r];
-            if (S.avg) V.x_acc[r] = ff_axpy(V.x_acc[r], S.w, xj);
-            const float v = fmaf(-S.tau, V.c[r] + pick(V.kty0, V.kty1, S.cur)[r], xj);
-            pick(V.x0, V.x1, S.cur ^ 1)[r] = fminf(fmaxf(v, V.l[r]), V.u[r]);
+    // chunks as for_each_element; every thread loads the operands of U = 4
+    // elements of its chunk before it stores any of them (the stores would
+    // otherwise keep the next element's loads behind them: one DRAM latency
+    // per element)
+    constexpr int U = 4;
+    const int nact = *ch.nactive;
+    for (int c = blockIdx.x; c < nact; c += gridDim.x) {
+        const int4 d = ch.chunks[ch.active[c]];  // begin, end, instance, is_col
+        const Inst& I = st[d.z];
+        if (I.done) continue;
+        const StepScalars S = step_scalars(I);
+        if (d.w) {
+            const float* xs = pick(V.x0, V.x1, S.cur);
+            const float* kt = pick(V.kty0, V.kty1, S.cur);
+            float* xn = pick(V.x0, V.x1, S.cur ^ 1);
+            for (int r0 = d.x + threadIdx.x; r0 < d.y; r0 += U * blockDim.x) {
+                float xv[U], cv[U], kv[U], lv[U], uv[U];
+                float2 av[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int r = r0 + u * blockDim.x;
+                    if (r < d.y) {
+                        xv[u] = xs[r];
+                        cv[u] = V.c[r];
+                        kv[u] = kt[r];
+                        lv[u] = V.l[r];
+                        uv[u] = V.u[r];
+                        if (S.avg) av[u] = V.x_acc[r];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int r = r0 + u * blockDim.x;
+                    if (r < d.y) {
+                        if (S.avg) V.x_acc[r] = ff_axpy(av[u], S.w, xv[u]);
+                        const float v = fmaf(-S.tau, cv[u] + kv[u], xv[u]);
+                        xn[r] = fminf(fmaxf(v, lv[u]), uv[u]);
+                    }
+                }
+            }
         } else if (S.avg) {
-            V.y_acc[r] = ff_axpy(V.y_acc[r], S.w, pick(V.y0, V.y1, S.cur)[r]);
+            const float* ys = pick(V.y0, V.y1, S.cur);
+            for (int r0 = d.x + threadIdx.x; r0 < d.y; r0 += U * blockDim.x) {
+                float yv[U];
+                float2 av[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int r = r0 + u * blockDim.x;
+                    if (r < d.y) {
+                        yv[u] = ys[r];
+                        av[u] = V.y_acc[r];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int r = r0 + u * blockDim.x;
+                    if (r < d.y) V.y_acc[r] = ff_axpy(av[u], S.w, yv[u]);
+                }
+            }
         }
-    });
+    }
+}
+
+// The step-size schedule factors k^-0.6 and k^-0.3 of this attempt (k =
+// attempts + 2) for the controller at the end of the A^T y kernel.  FP64 pow
+// is slow on this part: thread 0 of block b computes instances b, b + grid,
+// ... at the start of the A x kernel, whose other warps meanwhile take the
+// tasks (a kernel of this length hides it; the elementwise pass did not).
+__device__ __forceinline__ void step_schedule_pows(int B, Inst* __restrict__ st) {
+    if (threadIdx.x != 0) return;
+    for (int b = blockIdx.x; b < B; b += gridDim.x) {
+        Inst& S = st[b];
+        if (S.done) continue;
+        const double k = (double)(S.attempts + 2);
+        S.pow06 = pow(k, -0.6);
+        S.pow03 = pow(k, -0.3);
+    }
 }
 
 // Row epilogue of a step: K x' arrives as the dot product; dual update with
@@ -137,7 +194,8 @@ struct DualStepEpi {
     __device__ void finish(Inst& S, const double* tot) { S.dy2 = tot[0]; }
 };
 
-__global__ void __launch_bounds__(kThreads, 4) k_step_dual(Side rows, Vecs V, Inst* __restrict__ st) {
+__global__ void __launch_bounds__(kThreads, 4) k_step_dual(int B, Side rows, Vecs V, Inst* __restrict__ st) {
+    step_schedule_pows(B, st);
     DualStepEpi epi{V};
     spmv_engine<1, true, 1>(rows, st, epi, 0u);
 }
@@ -149,7 +207,7 @@ __device__ void step_controller(Inst& S, double dx2, double inter) {
     const double ai = fabs(inter);
     const double eta_bar = ai > 0.0 ? movement / (2.0 * ai) : INFINITY;
     // PDLP counts iterations from 1: the base k = attempts + 2 is at least 2;
-    // k^-0.6 and k^-0.3 were computed by k_step_primal of this step
+    // k^-0.6 and k^-0.3 were computed by the A x kernel of this step
     const double eta = S.eta;
     const double grow = (1.0 + S.pow06) * eta;
     const double eta_next = isinf(eta_bar) ? grow : fmin((1.0 - S.pow03) * eta_bar, grow);
@@ -226,8 +284,9 @@ struct KtyStepEpiStaged : KtyStepEpi {
 };
 
 __global__ void __launch_bounds__(kStagedThreads, 1)
-    k_step_dual_staged(Side rows, Vecs V, Inst* __restrict__ st, int staged) {
+    k_step_dual_staged(int B, Side rows, Vecs V, Inst* __restrict__ st, int staged) {
     stage_prefix(pick(V.x0, V.x1, st[0].cur ^ 1), staged);
+    step_schedule_pows(B, st);
     DualStepEpiStaged epi{{V}, staged};
     spmv_engine<1, true, 1>(rows, st, epi, 0u);
 }
@@ -1204,9 +1263,10 @@ void MixedSolver::launch_step_spmvs(cudaStream_t s, int which) {
     Inst* st = state_.as<Inst>();
     if (which == 1) {
         if (stage_x_ > 0)
-            k_step_dual_staged<<<sm_count_, kStagedThreads, sizeof(float) * stage_x_, s>>>(rows_, V_, st, stage_x_);
+            k_step_dual_staged<<<sm_count_, kStagedThreads, sizeof(float) * stage_x_, s>>>(B_, rows_, V_, st,
+                                                                                       stage_x_);
         else
-            k_step_dual<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
+            k_step_dual<<<grid_, kThreads, 0, s>>>(B_, rows_, V_, st);
     } else {
         if (stage_y_ > 0)
             k_step_kty_staged<<<sm_count_, kStagedThreads, sizeof(float) * stage_y_, s>>>(cols_, V_, st, stage_y_);
