@@ -85,12 +85,18 @@ __global__ void __launch_bounds__(kThreads) k_step_primal(int B, Chunks ch, Vecs
     // otherwise keep the next element's loads behind them: one DRAM latency
     // per element)
     constexpr int U = 4;
+    __shared__ StepScalars sh;
     const int nact = *ch.nactive;
     for (int c = blockIdx.x; c < nact; c += gridDim.x) {
         const int4 d = ch.chunks[ch.active[c]];  // begin, end, instance, is_col
         const Inst& I = st[d.z];
-        if (I.done) continue;
-        const StepScalars S = step_scalars(I);
+        if (I.done) continue;  // uniform over the block
+        // one thread turns the FP64 state into the chunk's scalars (an FP64
+        // division: per thread it would keep the slow FP64 pipe busy)
+        __syncthreads();
+        if (threadIdx.x == 0) sh = step_scalars(I);
+        __syncthreads();
+        const StepScalars S = sh;
         if (d.w) {
             const float* xs = pick(V.x0, V.x1, S.cur);
             const float* kt = pick(V.kty0, V.kty1, S.cur);
@@ -1489,10 +1495,23 @@ int MixedSolver::fetch(int b, std::vector<double>& x, std::vector<double>& y) {
     return SIH_PDHG_OK;
 }
 
+// Kernel timing: every instance with a step-weighted average update pending
+// (weight 1/2), as after an accepted step.
+__global__ void k_mark_average_pending(int B, Inst* __restrict__ st) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+        st[b].avg_pending = 1;
+        st[b].avg_w = 0.5;
+    }
+}
+
 int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
     SIHG_TRY(reset_state());
     cudaStream_t s = stream_;
     Inst* st = state_.as<Inst>();
+    // the state of an accepted step: an average update pending, so that the
+    // elementwise pass moves the float-float averages as it does in a solve
+    k_mark_average_pending<<<std::max(1, std::min(sm_count_, (B_ + 255) / 256)), 256, 0, s>>>(B_, st);
+    SIHG_LAUNCH_CHECK();
     cudaEvent_t e0, e1;
     SIHG_CUDA(cudaEventCreate(&e0));
     SIHG_CUDA(cudaEventCreate(&e1));

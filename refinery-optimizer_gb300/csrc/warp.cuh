@@ -74,8 +74,19 @@ struct Staged<Epi, decltype(void(Epi::kStaged))> {
 template <class Epi>
 __device__ __forceinline__ float gather_one(const Epi& epi, const float* __restrict__ vec, int idx) {
     if constexpr (Staged<Epi>::value) {
+        // predicated loads, no branch: the shared copy below `staged`, else
+        // the vector (the gathers of a batch then issue back to back)
         extern __shared__ float stage_vec[];
-        if (idx < epi.staged) return stage_vec[idx];
+        const unsigned saddr = (unsigned)__cvta_generic_to_shared(stage_vec) + 4u * (unsigned)idx;
+        float v;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.lt.s32 p, %1, %2;\n\t"
+            "@p ld.shared.f32 %0, [%3];\n\t"
+            "@!p ld.global.nc.f32 %0, [%4];\n\t}"
+            : "=f"(v)
+            : "r"(idx), "r"(epi.staged), "r"(saddr), "l"(vec + idx));
+        return v;
     }
     return ld_vec(vec + idx);
 }
@@ -415,18 +426,23 @@ __device__ __forceinline__ void spmv_engine(const Side& side, State* st, Epi& ep
 // Elementwise pass over every column (is_col) and row of the running
 // instances: blocks take chunks of kChunk consecutive elements of one
 // instance, threads stride through a chunk (coalesced).  `prep(S)` turns the
-// instance state into the chunk's scalars once (FP64 arithmetic and
-// conversions stay out of the element loop); `f(is_col, scalars, k)` does one
-// element.
+// instance state into the chunk's scalars once per block, on one thread
+// (FP64 arithmetic and conversions stay out of the element loop);
+// `f(is_col, scalars, k)` does one element.
 template <class State, class Prep, class F>
 __device__ __forceinline__ void for_each_element(const Chunks& ch, State* st, Prep&& prep, F&& f) {
+    using Scalars = decltype(prep(st[0]));
+    __shared__ Scalars sh;  // prep runs on one thread (FP64 is slow on this part)
     const int nact = *ch.nactive;
     for (int c = blockIdx.x; c < nact; c += gridDim.x) {
         const int4 d = ch.chunks[ch.active[c]];  // begin, end, instance, is_col
         const State& S = st[d.z];
-        if (S.done) continue;
+        if (S.done) continue;  // uniform over the block
         const bool is_col = d.w != 0;
-        const auto sc = prep(S);
+        __syncthreads();
+        if (threadIdx.x == 0) sh = prep(S);
+        __syncthreads();
+        const Scalars sc = sh;
         for (int r = d.x + threadIdx.x; r < d.y; r += blockDim.x) f(is_col, sc, r);
     }
 }

@@ -124,3 +124,40 @@ def test_renumbering_does_not_change_the_solution(sih):
     for s in (a, b):
         assert abs(s.primal_objective - ref) <= 40 * 1e-6 * (1 + abs(ref))
     np.testing.assert_allclose(a.x, b.x, atol=1e-3 * max(1.0, np.abs(b.x).max()))
+
+
+def test_staged_gathers_are_bit_identical(sih):
+    """options.staged_kib serves gathers below the staged prefix from a
+    shared-memory copy of the vector; the arithmetic is unchanged, so a solve
+    with staging (forced on both SpMVs, and automatic on a Zipf LP whose prefix
+    carries most nonzeros) returns the same point bit for bit."""
+    from sih_pdhg.generators import zipf_lp
+
+    prob = zipf_lp(20_000, 40_000, 480_000, seed=3)
+    cfg = sih.GpuPdhgConfig(max_iterations=3000, tol_primal=1e-4, tol_dual=1e-4, tol_gap=1e-4)
+    off = sih.solve_gpu_mixed(prob, cfg, staged_kib=-1)
+    for kib in (16, 0):
+        on = sih.solve_gpu_mixed(prob, cfg, staged_kib=kib)
+        assert on.status == off.status
+        assert on.simplex_iterations == off.simplex_iterations
+        np.testing.assert_array_equal(on.x, off.x)
+        np.testing.assert_array_equal(on.row_duals, off.row_duals)
+
+
+def test_staged_kib_above_the_device_limit_is_rejected(sih):
+    prob, _, _ = golden_case("rand_200x500_k8_s0")
+    cfg = sih.GpuPdhgConfig(max_iterations=1000, tol_primal=1e-4, tol_dual=1e-4, tol_gap=1e-4)
+    with pytest.raises(Exception, match="staged_kib"):
+        sih.solve_gpu_mixed(prob, cfg, staged_kib=100_000)
+
+
+@pytest.mark.parametrize("lanes", [(1, 1), (2, 4), (8, 2)])
+def test_lane_width_override_solves(sih, lanes):
+    """options.lanes_csr / lanes_csc fix the lanes per segment of the light
+    SpMV tasks; any power of two gives a correct solve."""
+    prob, entry, _ = golden_case("rand_2000x5000_k8_s0")
+    cfg = sih.GpuPdhgConfig(max_iterations=200000, tol_primal=1e-6, tol_dual=1e-6, tol_gap=1e-6)
+    s = sih.solve_gpu_mixed(prob, cfg, lanes_csr=lanes[0], lanes_csc=lanes[1])
+    assert s.is_optimal()
+    ref = entry["highs_objective"]
+    assert abs(s.primal_objective - ref) <= 40 * 1e-6 * (1 + abs(ref))
