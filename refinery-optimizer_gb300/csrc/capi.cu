@@ -1,4 +1,5 @@
 // C-ABI entry points (include/sih_pdhg.h).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -53,17 +54,33 @@ void pack_solution(const sih_pdhg_problem* p, const sih_pdhg_options& opts, cons
                    const std::vector<double>& y, sih_pdhg_result* r) {
     const int64_t m = p->num_rows, n = p->num_cols;
     KktReport k = host_kkt(p, x.data(), y.data(), r->slack, r->reduced_costs);
+    // objective and copies: per-thread partials, combined in thread order
+    const int T = std::max(1, hardware_threads());
+    std::vector<double> part(T, 0.0);
+    std::vector<char> fin(2 * (size_t)T, 1);
+    parallel_parts(n, T, [&](int64_t b, int64_t e, int t) {
+        double o = 0.0;
+        bool f = true;
+        for (int64_t j = b; j < e; ++j) {
+            o += p->c[j] * x[j];
+            f = f && std::isfinite(x[j]);
+            if (r->x) r->x[j] = x[j];
+        }
+        part[t] = o;
+        fin[t] = f;
+    });
+    parallel_parts(m, T, [&](int64_t b, int64_t e, int t) {
+        bool f = true;
+        for (int64_t i = b; i < e; ++i) {
+            f = f && std::isfinite(y[i]);
+            if (r->row_duals) r->row_duals[i] = opts.dual_sign ? -y[i] * p->sense : y[i];
+        }
+        fin[T + t] = f;
+    });
     double obj = 0.0;
     bool finite = true;
-    for (int64_t j = 0; j < n; ++j) {
-        obj += p->c[j] * x[j];
-        finite = finite && std::isfinite(x[j]);
-        if (r->x) r->x[j] = x[j];
-    }
-    for (int64_t i = 0; i < m; ++i) {
-        finite = finite && std::isfinite(y[i]);
-        if (r->row_duals) r->row_duals[i] = opts.dual_sign ? -y[i] * p->sense : y[i];
-    }
+    for (int t = 0; t < T; ++t) obj += part[t];
+    for (int t = 0; t < 2 * T; ++t) finite = finite && fin[t];
     r->primal_objective = obj + p->obj_offset;
     r->dual_bound = p->sense * k.dual_obj + p->obj_offset;
     r->rel_primal = k.rel_primal;

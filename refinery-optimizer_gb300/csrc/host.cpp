@@ -87,42 +87,50 @@ int build_host_problem(const sih_pdhg_problem* p, HostProblem& hp) {
     hp.u.resize(n);
     hp.rl.resize(m);
     hp.ru.resize(m);
-    for (int j = 0; j <= n && n > 0; ++j) hp.csc_ptr[j] = (int)p->csc_col_ptr[j];
-    if (n == 0) hp.csc_ptr[0] = 0;
-    std::atomic<int64_t> bad_index{-1};
-    parallel_for(nnz, [&](int64_t b, int64_t e) {
+    hp.csr_ptr.assign((size_t)m + 1, 0);
+    // pointers and vectors in one pass: items [0, n] are columns (n: the last
+    // pointer), items (n, n + 1 + m] rows
+    parallel_for((int64_t)n + 1 + m + 1, [&](int64_t b, int64_t e) {
         for (int64_t k = b; k < e; ++k) {
-            const int64_t r = p->csc_row_ind[k];
-            if (r < 0 || r >= m) bad_index.store(k);
-            hp.csc[k] = Pair{(int32_t)r, (float)p->csc_values[k]};
+            if (k <= n) {
+                const int64_t j = k;
+                hp.csc_ptr[j] = n > 0 ? (int)p->csc_col_ptr[j] : 0;
+                if (j < n) {
+                    hp.c[j] = (float)(p->sense == 1 ? p->c[j] : -p->c[j]);
+                    hp.l[j] = (float)p->col_lower[j];
+                    hp.u[j] = (float)p->col_upper[j];
+                }
+            } else {
+                const int64_t i = k - n - 1;
+                if (p->csr_row_ptr) hp.csr_ptr[i] = (int)p->csr_row_ptr[i];
+                if (i < m) {
+                    hp.rl[i] = (float)p->row_lower[i];
+                    hp.ru[i] = (float)p->row_upper[i];
+                }
+            }
         }
     });
-    if (bad_index.load() >= 0) return bad("csc_row_ind out of range at entry " + std::to_string(bad_index.load()));
-    const float sense = (float)p->sense;
-    for (int j = 0; j < n; ++j) {
-        hp.c[j] = (float)(p->sense == 1 ? p->c[j] : -p->c[j]);
-        hp.l[j] = (float)p->col_lower[j];
-        hp.u[j] = (float)p->col_upper[j];
-    }
-    (void)sense;
-    for (int i = 0; i < m; ++i) {
-        hp.rl[i] = (float)p->row_lower[i];
-        hp.ru[i] = (float)p->row_upper[i];
-    }
-    hp.csr_ptr.assign((size_t)m + 1, 0);
+    // entries: the CSC, and the CSR when the problem brings one, in one pass
+    // (items [0, nnz) CSC, [nnz, 2 nnz) CSR); every index is checked
     hp.csr.resize((size_t)nnz);
-    if (p->csr_row_ptr) {
-        for (int i = 0; i <= m; ++i) hp.csr_ptr[i] = (int)p->csr_row_ptr[i];
-        parallel_for(nnz, [&](int64_t b, int64_t e) {
-            for (int64_t k = b; k < e; ++k) {
-                const int64_t c = p->csr_col_ind[k];
-                if (c < 0 || c >= n) bad_index.store(k);
-                hp.csr[k] = Pair{(int32_t)c, (float)p->csr_values[k]};
+    std::atomic<int64_t> bad_csc{-1}, bad_csr{-1};
+    const int64_t items = p->csr_row_ptr ? 2 * (int64_t)nnz : (int64_t)nnz;
+    parallel_for(items, [&](int64_t b, int64_t e) {
+        for (int64_t k = b; k < e; ++k) {
+            if (k < nnz) {
+                const int64_t r = p->csc_row_ind[k];
+                if (r < 0 || r >= m) bad_csc.store(k);
+                hp.csc[k] = Pair{(int32_t)r, (float)p->csc_values[k]};
+            } else {
+                const int64_t q = k - nnz, c = p->csr_col_ind[q];
+                if (c < 0 || c >= n) bad_csr.store(q);
+                hp.csr[q] = Pair{(int32_t)c, (float)p->csr_values[q]};
             }
-        });
-        if (bad_index.load() >= 0)
-            return bad("csr_col_ind out of range at entry " + std::to_string(bad_index.load()));
-    } else {
+        }
+    });
+    if (bad_csc.load() >= 0) return bad("csc_row_ind out of range at entry " + std::to_string(bad_csc.load()));
+    if (bad_csr.load() >= 0) return bad("csr_col_ind out of range at entry " + std::to_string(bad_csr.load()));
+    if (!p->csr_row_ptr) {
         // Counting-sort transpose in column order (columns ascending within a row),
         // the CSR the reference builds at core/src/gpu/gpu_solver.cpp:91-109.
         for (int k = 0; k < nnz; ++k) hp.csr_ptr[hp.csc[k].idx + 1]++;
@@ -141,68 +149,71 @@ KktReport host_kkt(const sih_pdhg_problem* p, const double* x, const double* y, 
                    double* reduced_costs) {
     const int64_t m = p->num_rows, n = p->num_cols;
     const double sense = (double)p->sense;
-    std::vector<double> ax((size_t)m, 0.0);
-    if (p->csr_row_ptr) {
-        parallel_for(m, [&](int64_t b, int64_t e) {
-            for (int64_t i = b; i < e; ++i) {
-                double s = 0.0;
-                for (int64_t k = p->csr_row_ptr[i]; k < p->csr_row_ptr[i + 1]; ++k)
-                    s += p->csr_values[k] * x[p->csr_col_ind[k]];
-                ax[i] = s;
-            }
-        });
-    } else {
+    // A x: row by row from the problem's CSR, else one scatter pass over its CSC
+    std::vector<double> ax;
+    if (!p->csr_row_ptr) {
+        ax.assign((size_t)m, 0.0);
         for (int64_t j = 0; j < n; ++j)
             for (int64_t k = p->csc_col_ptr[j]; k < p->csc_col_ptr[j + 1]; ++k)
                 ax[p->csc_row_ind[k]] += p->csc_values[k] * x[j];
     }
-    const int T = hardware_threads();
-    std::vector<double> part_pobj(T, 0), part_dobj(T, 0), part_rd(T, 0), part_cinf(T, 0);
-    std::atomic<int> next{0};
+    // per-thread partials, combined in thread order (a fixed split per thread count)
+    struct Part {
+        double pobj = 0, dobj = 0, rd = 0, cinf = 0, rp = 0, binf = 0;
+    };
+    const int T = std::max(1, hardware_threads());
+    std::vector<Part> rows(T), cols(T);
+    auto row_work = [&](int64_t b, int64_t e, int t) {
+        Part& P = rows[t];
+        for (int64_t i = b; i < e; ++i) {
+            double a;
+            if (p->csr_row_ptr) {
+                a = 0.0;
+                for (int64_t k = p->csr_row_ptr[i]; k < p->csr_row_ptr[i + 1]; ++k)
+                    a += p->csr_values[k] * x[p->csr_col_ind[k]];
+            } else {
+                a = ax[i];
+            }
+            const double lo = p->row_lower[i], hi = p->row_upper[i];
+            double r = 0.0;
+            if (bound_is_finite(lo)) { P.binf = std::max(P.binf, std::fabs(lo)); if (a < lo) r = lo - a; }
+            if (bound_is_finite(hi)) { P.binf = std::max(P.binf, std::fabs(hi)); if (a > hi) r = a - hi; }
+            P.rp = std::max(P.rp, r);
+            const double yn = y[i] < 0 ? -y[i] : 0.0, yp = y[i] > 0 ? y[i] : 0.0;
+            if (bound_is_finite(lo)) P.dobj += yn * lo; else P.rd = std::max(P.rd, yn);
+            if (bound_is_finite(hi)) P.dobj -= yp * hi; else P.rd = std::max(P.rd, yp);
+            if (slack) slack[i] = a;
+        }
+    };
     auto col_work = [&](int64_t b, int64_t e, int t) {
-        double pobj = 0, dobj = 0, rd = 0, cinf = 0;
+        Part& P = cols[t];
         for (int64_t j = b; j < e; ++j) {
             const double cj = sense * p->c[j];
             double lam = cj;
             for (int64_t k = p->csc_col_ptr[j]; k < p->csc_col_ptr[j + 1]; ++k)
                 lam += p->csc_values[k] * y[p->csc_row_ind[k]];
             if (reduced_costs) reduced_costs[j] = sense * lam;
-            pobj += cj * x[j];
-            cinf = std::max(cinf, std::fabs(cj));
+            P.pobj += cj * x[j];
+            P.cinf = std::max(P.cinf, std::fabs(cj));
             const double pos = lam > 0 ? lam : 0.0, neg = lam < 0 ? -lam : 0.0;
-            if (bound_is_finite(p->col_lower[j])) dobj += pos * p->col_lower[j]; else rd = std::max(rd, pos);
-            if (bound_is_finite(p->col_upper[j])) dobj -= neg * p->col_upper[j]; else rd = std::max(rd, neg);
+            if (bound_is_finite(p->col_lower[j])) P.dobj += pos * p->col_lower[j]; else P.rd = std::max(P.rd, pos);
+            if (bound_is_finite(p->col_upper[j])) P.dobj -= neg * p->col_upper[j]; else P.rd = std::max(P.rd, neg);
         }
-        part_pobj[t] += pobj;
-        part_dobj[t] += dobj;
-        part_rd[t] = std::max(part_rd[t], rd);
-        part_cinf[t] = std::max(part_cinf[t], cinf);
     };
-    {
-        std::vector<std::thread> pool;
-        for (int t = 0; t < T; ++t)
-            pool.emplace_back([&, t] { col_work(n * t / T, n * (t + 1) / T, t); });
-        for (auto& th : pool) th.join();
-    }
-    (void)next;
-    double pobj = 0, dobj = 0, rd_inf = 0, c_inf = 0;
+    parallel_parts(n, T, col_work);
+    parallel_parts(m, T, row_work);
+    double pobj = 0, dobj = 0, rd_inf = 0, c_inf = 0, rp_inf = 0, b_inf = 0;
     for (int t = 0; t < T; ++t) {
-        pobj += part_pobj[t];
-        dobj += part_dobj[t];
-        rd_inf = std::max(rd_inf, part_rd[t]);
-        c_inf = std::max(c_inf, part_cinf[t]);
+        pobj += cols[t].pobj;
+        dobj += cols[t].dobj;
+        rd_inf = std::max(rd_inf, cols[t].rd);
+        c_inf = std::max(c_inf, cols[t].cinf);
     }
-    double rp_inf = 0, b_inf = 0;
-    for (int64_t i = 0; i < m; ++i) {
-        const double a = ax[i], lo = p->row_lower[i], hi = p->row_upper[i];
-        double r = 0.0;
-        if (bound_is_finite(lo)) { b_inf = std::max(b_inf, std::fabs(lo)); if (a < lo) r = lo - a; }
-        if (bound_is_finite(hi)) { b_inf = std::max(b_inf, std::fabs(hi)); if (a > hi) r = a - hi; }
-        rp_inf = std::max(rp_inf, r);
-        const double yn = y[i] < 0 ? -y[i] : 0.0, yp = y[i] > 0 ? y[i] : 0.0;
-        if (bound_is_finite(lo)) dobj += yn * lo; else rd_inf = std::max(rd_inf, yn);
-        if (bound_is_finite(hi)) dobj -= yp * hi; else rd_inf = std::max(rd_inf, yp);
-        if (slack) slack[i] = a;
+    for (int t = 0; t < T; ++t) {
+        dobj += rows[t].dobj;
+        rd_inf = std::max(rd_inf, rows[t].rd);
+        rp_inf = std::max(rp_inf, rows[t].rp);
+        b_inf = std::max(b_inf, rows[t].binf);
     }
     KktReport r;
     r.rel_primal = rp_inf / (1.0 + b_inf);

@@ -84,6 +84,12 @@ void parallel_for(int64_t count, F&& f) {
     parallel_for_min(count, (int64_t)1 << 16, static_cast<F&&>(f));
 }
 
+// Splits [0, count) into `parts` contiguous ranges (range t to part t) and runs
+// f(begin, end, t) on them in parallel; below 2 x 65,536 items everything runs
+// as part 0 on the calling thread.
+template <class F>
+void parallel_parts(int64_t count, int parts, F&& f);
+
 bool bound_is_finite(double v);
 int hardware_threads();
 
@@ -107,6 +113,21 @@ void parallel_for_min(int64_t count, int64_t min_chunk, F&& f) {
     for (int i = 0; i < t; ++i) {
         const int64_t b = count * i / t, e = count * (i + 1) / t;
         pool.emplace_back([&f, b, e] { f(b, e); });
+    }
+    for (auto& th : pool) th.join();
+}
+
+template <class F>
+void parallel_parts(int64_t count, int parts, F&& f) {
+    if (parts <= 1 || count < ((int64_t)1 << 17)) {
+        f((int64_t)0, count, 0);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(parts);
+    for (int t = 0; t < parts; ++t) {
+        const int64_t b = count * t / parts, e = count * (t + 1) / parts;
+        pool.emplace_back([&f, b, e, t] { f(b, e, t); });
     }
     for (auto& th : pool) th.join();
 }
