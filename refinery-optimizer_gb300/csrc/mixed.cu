@@ -45,6 +45,17 @@ namespace sihg {
 __device__ __forceinline__ float* pick(float* a, float* b, int sel) { return sel ? b : a; }
 __device__ __forceinline__ bool fin(float v) { return !isinf(v); }
 
+// Programmatic dependent launch.  The step kernels are launched with
+// programmatic stream serialization (launch_chained): their blocks may be
+// scheduled while the previous kernel in the stream finishes, and wait here,
+// before their first memory access, until it has completed and its writes are
+// visible; then they let the next kernel be scheduled.  Without the launch
+// attribute both instructions do nothing.
+__device__ __forceinline__ void chain_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // a - (s + e) for a float a and a float-float s + e, without losing the low part
 __device__ __forceinline__ float diff_ff(float a, float s, float e) {
     float h, l;
@@ -80,6 +91,7 @@ __device__ __forceinline__ StepScalars step_scalars(const Inst& S) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_step_primal(int B, Chunks ch, Vecs V, Inst* __restrict__ st) {
+    chain_wait();
     // chunks as for_each_element; every thread loads the operands of U = 4
     // elements of its chunk before it stores any of them (the stores would
     // otherwise keep the next element's loads behind them: one DRAM latency
@@ -201,6 +213,7 @@ struct DualStepEpi {
 };
 
 __global__ void __launch_bounds__(kThreads, 4) k_step_dual(int B, Side rows, Vecs V, Inst* __restrict__ st) {
+    chain_wait();
     step_schedule_pows(B, st);
     DualStepEpi epi{V};
     spmv_engine<1, true, 1>(rows, st, epi, 0u);
@@ -271,6 +284,7 @@ struct KtyStepEpi {
 };
 
 __global__ void __launch_bounds__(kThreads, 4) k_step_kty(Side cols, Vecs V, Inst* __restrict__ st) {
+    chain_wait();
     KtyStepEpi epi{V};
     spmv_engine<1, true, 2>(cols, st, epi, 0u);
 }
@@ -291,6 +305,7 @@ struct KtyStepEpiStaged : KtyStepEpi {
 
 __global__ void __launch_bounds__(kStagedThreads, 1)
     k_step_dual_staged(int B, Side rows, Vecs V, Inst* __restrict__ st, int staged) {
+    chain_wait();
     stage_prefix(pick(V.x0, V.x1, st[0].cur ^ 1), staged);
     step_schedule_pows(B, st);
     DualStepEpiStaged epi{{V}, staged};
@@ -299,6 +314,7 @@ __global__ void __launch_bounds__(kStagedThreads, 1)
 
 __global__ void __launch_bounds__(kStagedThreads, 1)
     k_step_kty_staged(Side cols, Vecs V, Inst* __restrict__ st, int staged) {
+    chain_wait();
     stage_prefix(pick(V.y0, V.y1, st[0].cur ^ 1), staged);
     KtyStepEpiStaged epi{{V}, staged};
     spmv_engine<1, true, 2>(cols, st, epi, 0u);
@@ -1253,32 +1269,52 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     return SIH_PDHG_OK;
 }
 
+// Launches a step kernel (which starts with chain_wait) with programmatic
+// stream serialization.
+template <class... P, class... A>
+static cudaError_t launch_chained(void (*kernel)(P...), int grid, int block, size_t smem, cudaStream_t s,
+                                  A... args) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 int MixedSolver::launch_step(cudaStream_t s) {
     launches_ += 3;
     Inst* st = state_.as<Inst>();
-    k_step_primal<<<elem_grid_, kThreads, 0, s>>>(B_, chunks_all_, V_, st);
-    launch_step_spmvs(s, 1);
-    launch_step_spmvs(s, 2);
+    SIHG_CUDA(launch_chained(k_step_primal, elem_grid_, kThreads, 0, s, B_, chunks_all_, V_, st));
+    SIHG_TRY(launch_step_spmvs(s, 1));
+    SIHG_TRY(launch_step_spmvs(s, 2));
     SIHG_LAUNCH_CHECK();
     return SIH_PDHG_OK;
 }
 
 // One of the step SpMVs (which = 1: K x' with the dual update, 2: K^T y' with
 // the step-size controller), staged when choose_staging picked a prefix.
-void MixedSolver::launch_step_spmvs(cudaStream_t s, int which) {
+int MixedSolver::launch_step_spmvs(cudaStream_t s, int which) {
     Inst* st = state_.as<Inst>();
     if (which == 1) {
         if (stage_x_ > 0)
-            k_step_dual_staged<<<sm_count_, kStagedThreads, sizeof(float) * stage_x_, s>>>(B_, rows_, V_, st,
-                                                                                       stage_x_);
+            SIHG_CUDA(launch_chained(k_step_dual_staged, sm_count_, kStagedThreads, sizeof(float) * stage_x_, s, B_,
+                                     rows_, V_, st, stage_x_));
         else
-            k_step_dual<<<grid_, kThreads, 0, s>>>(B_, rows_, V_, st);
+            SIHG_CUDA(launch_chained(k_step_dual, grid_, kThreads, 0, s, B_, rows_, V_, st));
     } else {
         if (stage_y_ > 0)
-            k_step_kty_staged<<<sm_count_, kStagedThreads, sizeof(float) * stage_y_, s>>>(cols_, V_, st, stage_y_);
+            SIHG_CUDA(launch_chained(k_step_kty_staged, sm_count_, kStagedThreads, sizeof(float) * stage_y_, s,
+                                     cols_, V_, st, stage_y_));
         else
-            k_step_kty<<<grid_, kThreads, 0, s>>>(cols_, V_, st);
+            SIHG_CUDA(launch_chained(k_step_kty, grid_, kThreads, 0, s, cols_, V_, st));
     }
+    return SIH_PDHG_OK;
 }
 
 // Staged gathers (single LP): the first entries of the gathered vector that
@@ -1519,8 +1555,17 @@ int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
     for (int k = 0; k < 3 && rc == SIH_PDHG_OK; ++k) {
         cudaEventRecord(e0, s);
         for (int i = 0; i < reps; ++i) {
-            if (k == 0) k_step_primal<<<elem_grid_, kThreads, 0, s>>>(B_, chunks_all_, V_, st);
-            if (k > 0) launch_step_spmvs(s, k);
+            int r = SIH_PDHG_OK;
+            if (k == 0) {
+                const cudaError_t e = launch_chained(k_step_primal, elem_grid_, kThreads, 0, s, B_, chunks_all_, V_, st);
+                if (e != cudaSuccess) r = cuda_fail(e, "k_step_primal launch", __FILE__, __LINE__);
+            } else {
+                r = launch_step_spmvs(s, k);
+            }
+            if (r != SIH_PDHG_OK) {
+                rc = r;
+                break;
+            }
         }
         cudaEventRecord(e1, s);
         cudaError_t e = cudaEventSynchronize(e1);

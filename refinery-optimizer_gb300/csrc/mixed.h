@@ -173,7 +173,7 @@ class MixedSolver {
     int launch_compact(cudaStream_t s);
     int record_graph();
     int choose_staging();
-    void launch_step_spmvs(cudaStream_t s, int which);
+    int launch_step_spmvs(cudaStream_t s, int which);
 
     std::vector<const HostProblem*> probs_;
     sih_pdhg_config cfg_{};
