@@ -97,6 +97,51 @@ def random_feasible_lp(m: int, n: int, counts, seed: int = 0, m_eq: int | None =
                                ObjectiveSense.Minimize, 0.0, name)
 
 
+def mixed_bounds_lp(m: int = 80, n: int = 200, nnz_per_col: int = 4, seed: int = 0) -> Problem:
+    """Small LP with every kind of row and column bound, feasible and bounded by
+    construction: rows cycle through equality, <=, >=, ranged and free (no
+    finite bound), columns through boxed [0, U], lower-only, upper-only, free
+    and fixed (lower == upper); the last row and the last column hold no
+    nonzeros (the row's bounds [-1, 1] contain its activity 0).  A point x0
+    inside the column bounds sets the row bounds around A x0; duals y0 with the
+    row types' signs (>= 0 on >= rows, <= 0 on <= rows, 0 on free rows) and a
+    reduced cost s with the column types' signs (>= 0 lower-only, <= 0
+    upper-only, 0 free) give c = A^T y0 + s, a dual feasible point."""
+    rng = np.random.default_rng(seed)
+    counts = np.full(n, nnz_per_col, dtype=np.int64)
+    counts[-1] = 0
+    cols, rows = _distinct_rows(rng, counts, m - 1)  # the last row stays empty
+    vals = rng.standard_normal(rows.shape[0])
+    cp = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=cp[1:])
+    ctype = np.arange(n) % 5          # 0 boxed, 1 lower-only, 2 upper-only, 3 free, 4 fixed
+    ctype[-1] = 0
+    U = rng.uniform(1.0, 10.0, n)
+    lo_b = rng.uniform(-2.0, 0.0, n)
+    up_b = rng.uniform(0.0, 5.0, n)
+    col_lower = np.where(ctype == 0, 0.0, np.where(ctype == 1, lo_b, np.where(ctype == 4, lo_b, -INF)))
+    col_upper = np.where(ctype == 0, U, np.where(ctype == 2, up_b, np.where(ctype == 4, lo_b, INF)))
+    spread = rng.uniform(0.0, 3.0, n)
+    x0 = np.select([ctype == 0, ctype == 1, ctype == 2, ctype == 3, ctype == 4],
+                   [rng.uniform(0.0, 1.0, n) * U, lo_b + spread, up_b - spread, rng.normal(0.0, 3.0, n), lo_b])
+    ax0 = np.bincount(rows, weights=vals * x0[cols], minlength=m)
+    rtype = np.arange(m) % 5          # 0 equality, 1 <=, 2 >=, 3 ranged, 4 free
+    rtype[-1] = 3
+    gap_lo, gap_up = rng.uniform(0.0, 1.0, m), rng.uniform(0.0, 1.0, m)
+    row_lower = np.select([rtype == 0, rtype == 2, rtype == 3], [ax0, ax0 - gap_lo, ax0 - gap_lo], -INF)
+    row_upper = np.select([rtype == 0, rtype == 1, rtype == 3], [ax0, ax0 + gap_up, ax0 + gap_up], INF)
+    row_lower[-1], row_upper[-1] = -1.0, 1.0
+    yn = rng.standard_normal(m)
+    y0 = np.select([rtype == 1, rtype == 2, rtype == 4], [-np.abs(yn), np.abs(yn), 0.0], yn)
+    sn = rng.standard_normal(n)
+    su = rng.uniform(0.0, 1.0, n)
+    s = np.select([ctype == 1, ctype == 2, ctype == 3], [su, -su, 0.0], sn)
+    c = np.bincount(cols, weights=vals * y0[rows], minlength=n) + s
+    rp, ci, rv = csc_to_csr(m, n, cp, rows, vals)
+    A = SparseMatrix(m, n, cp, rows, vals, rp, ci, rv)
+    return Problem.from_arrays(A, c, col_lower, col_upper, row_lower, row_upper, ObjectiveSense.Minimize, 0.0,
+                               f"mixed_bounds_{m}x{n}_s{seed}")
+
 def small_random_lp(m: int = 2000, n: int = 5000, nnz_per_col: int = 8, seed: int = 0) -> Problem:
     """m rows (first half equalities, rest <=), n columns, exactly ``nnz_per_col``
     nonzeros per column.  Defaults are the 2,000 x 5,000 / 40k-nnz instance."""

@@ -54,6 +54,25 @@ def golden_config(name: str):
     return cfg
 
 
+def highs_general(problem):
+    """FP64 HiGHS (scipy, dual simplex) optimum of a minimisation LP with any mix
+    of finite and infinite row and column bounds: (objective, x).  Test oracle only."""
+    sp = pytest.importorskip("scipy.sparse")
+    from scipy.optimize import linprog
+
+    p = problem
+    A = sp.csc_matrix((p.A.csc_values(), p.A.csc_row_ind(), p.A.csc_col_ptr()), shape=(p.num_rows(), p.num_cols()))
+    rl, ru = p.row_lower, p.row_upper
+    eq = rl == ru
+    ub = (~eq) & np.isfinite(ru)
+    lb = (~eq) & np.isfinite(rl)
+    bounds = [(a if np.isfinite(a) else None, b if np.isfinite(b) else None) for a, b in zip(p.col_lower, p.col_upper)]
+    r = linprog(p.c, A_ub=sp.vstack([A[ub], -A[lb]]).tocsc(), b_ub=np.concatenate([ru[ub], -rl[lb]]),
+                A_eq=A[eq], b_eq=rl[eq], bounds=bounds, method="highs-ds")
+    assert r.status == 0, r.message
+    return float(r.fun), r.x
+
+
 @pytest.fixture(scope="session")
 def oracle_lib():
     import oracle
