@@ -119,7 +119,7 @@ typedef struct sih_pdhg_options {
     double restart_sufficient; /* mixed: 0.2 */
     double restart_necessary;  /* mixed: 0.8 */
     double restart_artificial; /* mixed: 0.36 */
-    double primal_weight_smoothing; /* mixed: 0.5 */
+    double primal_weight_smoothing; /* mixed: 0.5 (PDLP); 0.8 adapts faster (refinery LPs) */
     int32_t exact_arithmetic;  /* plain: 1 = the reference kernels' arithmetic (one thread per row/column,
                                   entry-order sums, no fused multiply-add); results then equal the CPU
                                   restatement bit for bit.  0 = warp-cooperative SpMV with FMA (default) */

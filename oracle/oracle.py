@@ -149,14 +149,16 @@ class PdlpInfo(C.Structure):
 
 
 def pdlp_solve(problem, max_attempts=100000, tol=1e-4, tol_p=None, tol_d=None, tol_g=None, eval_frequency=64,
-               ruiz_iterations=10, pock_chambolle=1, enable_restart=1, fp32_bits=0):
-    """FP64 restarted adaptive PDHG (the algorithm of the mixed CUDA path).
+               ruiz_iterations=10, pock_chambolle=1, enable_restart=1, fp32_bits=0, weight_smoothing=0.5,
+               restart_sufficient=0.2, restart_necessary=0.8, restart_artificial=0.36):
+    """FP64 restarted adaptive PDHG (the algorithm of the mixed CUDA path, with its
+    default options: primal weight smoothing 0.5, restart thresholds 0.2 / 0.8 / 0.36).
     Returns (x, y_pdhg, info dict); a maximization problem is solved as min -c."""
     A = problem.A
     m, n = problem.num_rows(), problem.num_cols()
     o = PdlpOpts(ruiz_iterations, pock_chambolle, eval_frequency, enable_restart, max_attempts,
                  tol if tol_p is None else tol_p, tol if tol_d is None else tol_d, tol if tol_g is None else tol_g,
-                 0.2, 0.8, 0.36, 0.5, fp32_bits)
+                 restart_sufficient, restart_necessary, restart_artificial, weight_smoothing, fp32_bits)
     c = np.ascontiguousarray(problem.c * (1 if int(problem.sense) == 1 else -1), dtype=np.float64)
     x = np.zeros(n)
     y = np.zeros(m)

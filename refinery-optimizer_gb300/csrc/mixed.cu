@@ -16,8 +16,9 @@
 //             step-weighted average iterate; restart to the better one on
 //             sufficient (0.2), necessary-without-progress (0.8) or artificial
 //             (0.36 of all steps) decay of the weighted KKT error;
-//   weight    at a restart omega <- exp(0.5 log(|dy|/|dx|) + 0.5 log omega)
-//             from the distances moved since the previous restart;
+//   weight    at a restart omega <- exp(th log(|dy|/|dx|) + (1 - th) log omega)
+//             from the distances moved since the previous restart, th =
+//             `primal_weight_smoothing` (PDLP's 0.5 by default);
 //   stop      relative KKT of docs/gpu_pdhg.md:51-57 (inf-norms, original
 //             space) of the current or average point <= tolerances.
 // Precision: matrix, iterates and SpMV products in FP32; every reduction

@@ -39,7 +39,7 @@ def test_reduce_max_and_seeds_world_size_2():
     import torch.multiprocessing as mp
 
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of this (multi-threaded) process
     out = mgr.dict()
     mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
     assert out[0][0] == out[1][0] == 1.0
