@@ -213,7 +213,7 @@ def measured_hbm_peak():
 
 
 # ------------------------------------------------------------------ CPU baselines (oracle = test/baseline only)
-def cpu_pdlp_sample(problem, gpu_attempts: int, budget_s: float) -> dict:
+def cpu_pdlp_sample(problem, gpu_attempts: int, sample_s: float) -> dict:
     """FP64 CPU port of the same mixed algorithm (oracle/pdlp_oracle.c, one
     thread) on a bounded number of steps, scaled to the GPU's step count."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -224,7 +224,7 @@ def cpu_pdlp_sample(problem, gpu_attempts: int, budget_s: float) -> dict:
     t0 = time.perf_counter()
     oracle.pdlp_solve(problem, max_attempts=attempts, tol=1e-30)
     dt = time.perf_counter() - t0
-    while dt < budget_s / 3 and attempts < 4096:
+    while dt < sample_s / 3 and attempts < 4096:
         attempts *= 2
         t0 = time.perf_counter()
         oracle.pdlp_solve(problem, max_attempts=attempts, tol=1e-30)

@@ -32,7 +32,7 @@ enum {
     SIH_PDHG_ERR_NO_DEVICE = 2,        /* no CUDA device: the engine has no CPU fallback */
     SIH_PDHG_ERR_CUDA = 3,             /* a CUDA runtime call or kernel launch failed */
     SIH_PDHG_ERR_OUT_OF_MEMORY = 4,    /* device or pinned-host allocation failed */
-    SIH_PDHG_ERR_UNSUPPORTED = 5       /* valid request this build cannot serve (e.g. > 2^31-1 nnz) */
+    SIH_PDHG_ERR_UNSUPPORTED = 5       /* valid request the library cannot serve (e.g. > 2^31-1 nnz) */
 };
 
 /* ---- values of sih::model::SolutionStatus (core/include/sih/model/solution.hpp:11-21) */

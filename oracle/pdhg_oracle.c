@@ -2,7 +2,7 @@
  * CPU oracle for the GPU PDHG path -- TEST INFRASTRUCTURE ONLY.
  *
  * This file is a plain-C restatement of the reference's GPU PDHG solve.  It is
- * the checker that the CUDA path is compared against (tests, smoke check) and
+ * the reference the CUDA path is compared against (tests, smoke check) and
  * the CPU baseline that the benchmark times beside it.  Nothing in the shipped
  * library links, loads or calls it.
  *

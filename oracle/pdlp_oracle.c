@@ -1,6 +1,6 @@
 /*
  * FP64 CPU oracle of the mixed-precision restarted adaptive PDHG -- TEST
- * INFRASTRUCTURE ONLY (checker for the CUDA path; nothing ships it).
+ * INFRASTRUCTURE ONLY (what the CUDA path is compared against; nothing ships it).
  *
  * The reference's GPU path does not implement the adaptive pieces that its
  * own design document asks for (docs/gpu_pdhg.md:42-57: equilibration,
