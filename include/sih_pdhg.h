@@ -329,6 +329,26 @@ int sih_pdhg_adjoint_batch(const sih_pdhg_problem* problems, int32_t count, cons
                            double* const* grad_col_lower, double* const* grad_col_upper,
                            const sih_pdhg_adjoint_options* opts, sih_pdhg_adjoint_info* info);
 
+/* ---- problem ingest: MPS files --------------------------------------------
+ * Replaces sih::io::read_mps (core/src/io/mps_io.cpp:63-323) on the way into
+ * this engine: same records, same problem (row and column bounds, objective,
+ * sense, offset, duplicate entries summed and |a| <= 1e-15 dropped as
+ * SparseMatrix::from_triplets does, core/src/model/sparse_matrix.cpp:13-88),
+ * with CSC and CSR built in one pass instead of a coordinate map.  Integer
+ * markers and BV / UI / LI bounds are counted (the PDHG solve takes the LP
+ * relaxation, as the reference's does); a QUADOBJ / QMATRIX section returns
+ * SIH_PDHG_ERR_UNSUPPORTED.  Parse errors (a token that is not a number,
+ * contradictory bounds) return SIH_PDHG_ERR_INVALID_ARGUMENT with the line or
+ * the row / column in the message; the reference throws instead.
+ * The handle owns every array; sih_pdhg_mps_view points a sih_pdhg_problem
+ * (CSC and CSR filled) into them, valid until sih_pdhg_mps_free. */
+typedef struct sih_pdhg_mps sih_pdhg_mps;
+int sih_pdhg_read_mps(const char* path, sih_pdhg_mps** out);
+int sih_pdhg_read_mps_text(const char* text, size_t length, sih_pdhg_mps** out); /* same, from memory */
+int sih_pdhg_mps_view(const sih_pdhg_mps* mps, sih_pdhg_problem* problem, const char** name,
+                      int64_t* integer_columns); /* name and integer_columns may be NULL */
+void sih_pdhg_mps_free(sih_pdhg_mps* mps);
+
 /* ---- convergence check without allocation ---------------------------------
  * No counterpart in the reference.  For callers that must not allocate device
  * memory while they run (a host that hands every library a fixed device pool

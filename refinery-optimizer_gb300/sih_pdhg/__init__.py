@@ -5,7 +5,9 @@ Drop-in for the GPU PDHG path of the reference's ``sih_solver`` package
 ``GpuSolver.is_cuda_available``, ``GpuSolver.get_vram_info``,
 ``solve_gpu_pdhg`` and ``GpuPdhgConfig`` keep their names and meaning, over the
 C ABI of include/sih_pdhg.h.  Added: ``GpuSolver.solve_ex`` / ``solve_gpu_mixed``
-(mixed-precision restarted adaptive PDHG).
+(mixed-precision restarted adaptive PDHG), ``read_mps`` (the reference's
+``sih_solver.read_mps`` records, core/src/io/mps_io.cpp:63-323, read by the
+engine's one-pass MPS reader).
 """
 from __future__ import annotations
 
@@ -18,11 +20,13 @@ import numpy as np
 from . import _lib
 from ._lib import ALGO_MIXED, ALGO_PLAIN, SihPdhgError, default_options
 from .config import GpuPdhgConfig
+from .mps import write_mps
 from .problem import INF, ObjectiveSense, Problem, Solution, SolutionStatus, SparseMatrix
 
 __all__ = ["GpuSolver", "GpuPdhgConfig", "GpuMemoryInfo", "Problem", "SparseMatrix", "Solution",
            "SolutionStatus", "ObjectiveSense", "solve_gpu_pdhg", "solve_gpu_mixed", "solve_batch", "PdhgHandle",
-           "default_options", "SihPdhgError", "ALGO_PLAIN", "ALGO_MIXED", "INF", "adjoint_batch", "polish_batch"]
+           "default_options", "SihPdhgError", "ALGO_PLAIN", "ALGO_MIXED", "INF", "adjoint_batch", "polish_batch",
+           "read_mps", "read_mps_text", "write_mps"]
 
 
 @dataclass
@@ -220,6 +224,54 @@ def polish_batch(problems, xs, row_duals, tolerance: float = 1e-6, max_iteration
     del keep
     return xo, yo, [{k: getattr(infos[i], k) for k, _ in _lib.CPolishInfo._fields_ if k != "reserved"}
                     for i in range(B)]
+
+
+
+def _problem_from_mps(handle) -> Problem:
+    lib = _lib.load()
+    view = _lib.CProblem()
+    name = C.c_char_p()
+    ints = C.c_int64()
+    try:
+        _lib.check(lib.sih_pdhg_mps_view(handle, C.byref(view), C.byref(name), C.byref(ints)))
+        m, n, nnz = view.num_rows, view.num_cols, view.num_nonzeros
+
+        def arr(ptr, count, ctype):
+            if count == 0:
+                return np.zeros(0, dtype=np.int64 if ctype is C.c_int64 else np.float64)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), shape=(count,)).copy()
+
+        A = SparseMatrix(m, n, arr(view.csc_col_ptr, n + 1, C.c_int64), arr(view.csc_row_ind, nnz, C.c_int64),
+                         arr(view.csc_values, nnz, C.c_double), arr(view.csr_row_ptr, m + 1, C.c_int64),
+                         arr(view.csr_col_ind, nnz, C.c_int64), arr(view.csr_values, nnz, C.c_double))
+        p = Problem.from_arrays(A, arr(view.c, n, C.c_double), arr(view.col_lower, n, C.c_double),
+                                arr(view.col_upper, n, C.c_double), arr(view.row_lower, m, C.c_double),
+                                arr(view.row_upper, m, C.c_double), ObjectiveSense(view.sense), view.obj_offset,
+                                (name.value or b"").decode(errors="replace"))
+        p.integer_columns = int(ints.value)
+        return p
+    finally:
+        lib.sih_pdhg_mps_free(handle)
+
+
+def read_mps(path) -> Problem:
+    """Problem of an MPS file (sih_pdhg_read_mps): the records of the reference's
+    reader, CSC and CSR filled.  ``problem.integer_columns`` counts integer
+    columns (solved as their LP relaxation).  Raises SihPdhgError on a parse
+    error or a quadratic objective."""
+    lib = _lib.load()
+    h = C.c_void_p()
+    _lib.check(lib.sih_pdhg_read_mps(str(path).encode(), C.byref(h)))
+    return _problem_from_mps(h)
+
+
+def read_mps_text(text) -> Problem:
+    """read_mps of an MPS text held in memory (str or bytes)."""
+    lib = _lib.load()
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    h = C.c_void_p()
+    _lib.check(lib.sih_pdhg_read_mps_text(data, len(data), C.byref(h)))
+    return _problem_from_mps(h)
 
 
 class GpuSolver:

@@ -123,6 +123,12 @@ def load() -> C.CDLL:
     lib.sih_pdhg_check_norms_noalloc.argtypes = [i32, i32, i32] + [vp] * 14 + [C.c_float, C.c_float, vp, vp]
     lib.sih_pdhg_solve_batch.argtypes = [C.POINTER(CProblem), C.c_int32, C.POINTER(GpuPdhgConfig),
                                          C.POINTER(COptions), C.POINTER(CResult)]
+    lib.sih_pdhg_read_mps.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    lib.sih_pdhg_read_mps_text.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(C.c_void_p)]
+    lib.sih_pdhg_mps_view.argtypes = [C.c_void_p, C.POINTER(CProblem), C.POINTER(C.c_char_p),
+                                      C.POINTER(C.c_int64)]
+    lib.sih_pdhg_mps_free.argtypes = [C.c_void_p]
+    lib.sih_pdhg_mps_free.restype = None
     _lib = lib
     return lib
 

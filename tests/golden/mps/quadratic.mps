@@ -1,0 +1,11 @@
+NAME quadratic
+ROWS
+ N  OBJ
+ L  R1
+COLUMNS
+    A         OBJ        1.0      R1         1.0
+RHS
+    RHS       R1         1.0
+QUADOBJ
+    A         A          2.0
+ENDATA
