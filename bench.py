@@ -23,6 +23,8 @@ Workloads (seeded synthetic LPs, FP64 data, generators in sih_pdhg.generators):
                  scenarios on the same GPU (sampled) for the batched-vs-plain ratio
   refinery-64    the first 64 of those scenarios (a shorter batch)
   random-2kx5k-x256  256 instances of the 2,000 x 5,000 LP (seeds 0..255) as one batch
+  mps:PATH       the LP of an MPS file (sih_pdhg.read_mps); the reference arm prints
+                 an `unavailable` line for it (no measured plain iteration count)
 
 Multi-GPU: replicas (each rank solves its own copy of a single LP, or its own
 seeded batch of a batch workload; no data-path exchange; scaling "weak").
@@ -81,9 +83,14 @@ WORKLOADS = ["zipf-500kx1m", "random-2kx5k", "refinery-168p", "refinery-512", "r
 
 
 def make_workload(name: str, seed: int = 0):
-    """The workload's LP, or its list of LPs for a batch workload."""
+    """The workload's LP, or its list of LPs for a batch workload.  ``mps:PATH``
+    reads the LP of an MPS file (sih_pdhg.read_mps)."""
     from sih_pdhg.generators import refinery_lp, refinery_scenarios, small_random_lp, zipf_lp
 
+    if name.startswith("mps:"):
+        import sih_pdhg
+
+        return sih_pdhg.read_mps(name[4:])
     if name == "zipf-500kx1m":
         return zipf_lp(500_000, 1_000_000, 12_000_000, seed)
     if name == "random-2kx5k":
@@ -108,7 +115,8 @@ def parse_args():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="zipf-500kx1m", choices=WORKLOADS)
+    ap.add_argument("--workload", default="zipf-500kx1m",
+                    help=f"one of {', '.join(WORKLOADS)}, or mps:PATH (the LP of an MPS file)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tol", type=float, default=1e-4)
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
@@ -121,7 +129,10 @@ def parse_args():
                          "(no CUDA graph), then exit; prints no bench line")
     ap.add_argument("--profile-algorithm", default="mixed", choices=["mixed", "plain"],
                     help="algorithm of --profile-solve: mixed, or plain (the reference's FP32 PDHG)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.workload not in WORKLOADS and not args.workload.startswith("mps:"):
+        ap.error(f"unknown workload {args.workload}")
+    return args
 
 
 def run_profile_solve(args) -> None:
@@ -252,6 +263,10 @@ def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    if args.workload.startswith("mps:"):
+        print(json.dumps({"impl": "reference", "unavailable": "the iterations the reference algorithm needs on an "
+                          "arbitrary MPS file are not known (they are measured per workload)"}), flush=True)
+        return
     work = make_workload(args.workload)
     probs = as_list(work)
     prob = probs[0]
@@ -378,7 +393,9 @@ def run_gb300(args) -> None:
     line = {
         "metric": METRIC, "value": step, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded generator, seed 0)",
+        "vs_baseline": None, "dtype": "f32+f64",
+        "data": (f"MPS file {args.workload[4:]}" if args.workload.startswith("mps:")
+                 else "synthetic (seeded generator, seed 0)"),
         "config": cfg_desc,
         "iterations": max(iters), "restarts": sols[0].restarts,
         "status": max(int(s.status) for s in sols),

@@ -61,3 +61,14 @@ def test_reference_arm_under_torchrun_world_size_2():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_on_an_mps_workload_reports_unavailable():
+    """`--workload mps:PATH` reads an MPS file; the reference arm has no measured
+    iteration count for it and says so in its one JSON line (exit 0)."""
+    path = os.path.join(REPO, "tests", "golden", "mps", "edge_values.mps")
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--workload",
+                        f"mps:{path}"], capture_output=True, text=True, timeout=300, cwd=REPO)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
+    assert d["impl"] == "reference" and "unavailable" in d
