@@ -171,6 +171,7 @@ class Problem:
         self.row_upper = np.zeros(0)
         self.col_lower = np.zeros(0)
         self.col_upper = np.zeros(0)
+        self.integer_columns = 0  # integer columns of an MPS file (solved as their LP relaxation)
 
     @staticmethod
     def from_arrays(A: SparseMatrix, c, col_lower, col_upper, row_lower, row_upper,
