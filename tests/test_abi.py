@@ -163,3 +163,67 @@ def test_polish_host_path_runs_without_a_device():
     with pytest.raises(sih_pdhg.SihPdhgError) as e:
         sih_pdhg.polish_batch([p], [x], [y])
     assert e.value.code == 2
+
+
+C_CLIENT = r"""
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include "sih_pdhg.h"
+
+int main(int argc, char** argv) {
+    sih_pdhg_mps* mps = NULL;
+    if (sih_pdhg_read_mps(argv[1], &mps) != SIH_PDHG_OK) { printf("read %s\n", sih_pdhg_last_error()); return 1; }
+    sih_pdhg_problem p;
+    const char* name = NULL;
+    int64_t ints = -1;
+    if (sih_pdhg_mps_view(mps, &p, &name, &ints) != SIH_PDHG_OK) return 2;
+    printf("problem %s %lld %lld %lld %lld %d %g\n", name, (long long)p.num_rows, (long long)p.num_cols,
+           (long long)p.num_nonzeros, (long long)ints, p.sense, p.obj_offset);
+    sih_pdhg_config cfg;
+    sih_pdhg_config_default(&cfg);
+    sih_pdhg_options opt;
+    sih_pdhg_options_default(&opt);
+    opt.algorithm = SIH_PDHG_ALGO_MIXED;
+    double* x = calloc((size_t)p.num_cols, sizeof(double));
+    double* y = calloc((size_t)p.num_rows, sizeof(double));
+    sih_pdhg_result r = {0};
+    r.x = x;
+    r.row_duals = y;
+    int rc = sih_pdhg_solve_ex(&p, &cfg, &opt, &r);
+    printf("solve %d %d %.9g\n", rc, r.status, r.primal_objective);
+    free(x);
+    free(y);
+    sih_pdhg_mps_free(mps);
+    return 0;
+}
+"""
+
+
+def test_plain_c_client_reads_mps_and_calls_the_solver(tmp_path):
+    """The ABI from C (no C++ or Python in between): read an MPS file into a
+    sih_pdhg_problem view and hand it to sih_pdhg_solve_ex.  Without a device
+    the solve returns SIH_PDHG_ERR_NO_DEVICE after the problem was accepted;
+    with one it solves (min -x1 - 2 x2, x1 + x2 <= 4, x1 - x2 <= -1, x >= 0:
+    optimum -8 at (0, 4))."""
+    from sih_pdhg import _lib
+
+    lib_path = _lib.LIB_PATH
+    src = tmp_path / "client.c"
+    src.write_text(C_CLIENT)
+    exe = tmp_path / "client"
+    subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Werror", "-I", HEADER_DIR, str(src), "-o", str(exe),
+                           lib_path, f"-Wl,-rpath,{os.path.dirname(lib_path)}", "-lm"])
+    mps = tmp_path / "toy.mps"
+    mps.write_text("NAME toy\nROWS\n N  OBJ\n L  R1\n L  R2\nCOLUMNS\n    X1  OBJ  -1.0  R1  1.0\n"
+                   "    X1  R2  1.0\n    X2  OBJ  -2.0  R1  1.0\n    X2  R2  -1.0\nRHS\n    RHS  R1  4.0  R2  -1.0\n"
+                   "ENDATA\n")
+    out = subprocess.run([str(exe), str(mps)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stdout + out.stderr
+    lines = dict(l.split(" ", 1) for l in out.stdout.splitlines())
+    assert lines["problem"] == "toy 2 2 4 0 1 0"
+    rc, status, obj = lines["solve"].split()
+    if int(rc) == 2:  # SIH_PDHG_ERR_NO_DEVICE: validation passed, no CPU fallback
+        return
+    assert int(rc) == 0 and int(status) == 0
+    assert abs(float(obj) - (-8.0)) <= 1e-3
