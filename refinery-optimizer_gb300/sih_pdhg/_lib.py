@@ -17,6 +17,7 @@ PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.environ.get("SIH_PDHG_LIB") or os.path.join(PKG_DIR, "_build", "libsih_pdhg.so")
 
 OK = 0
+ABI_VERSION = 1  # SIH_PDHG_ABI_VERSION of include/sih_pdhg.h that these ctypes layouts mirror
 ERR_NAMES = {1: "invalid argument", 2: "no CUDA device", 3: "CUDA error", 4: "out of memory", 5: "unsupported"}
 
 ALGO_PLAIN = 0
@@ -91,6 +92,9 @@ def load() -> C.CDLL:
     lib = C.CDLL(LIB_PATH)
     vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
     lib.sih_pdhg_abi_version.restype = i32
+    if lib.sih_pdhg_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{LIB_PATH} has ABI version {lib.sih_pdhg_abi_version()}, this binding expects "
+                           f"{ABI_VERSION}: rebuild the library")
     lib.sih_pdhg_last_error.restype = C.c_char_p
     lib.sih_pdhg_is_cuda_available.restype = i32
     lib.sih_pdhg_get_vram_info.argtypes = [C.POINTER(C.c_uint64)] * 3
