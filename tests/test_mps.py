@@ -8,13 +8,13 @@
   tests/golden/make_mps_golden.py), and fails where it failed;
 * round trips: write_mps then read_mps gives back the generators' LPs;
 * with the reference build present (this container): the reference's toy LP
-  and MILP files and generated LPs read the same through both readers.
+  and MILP files, generated LPs and 200 seeded random MPS texts read the same
+  through both readers (or fail in both).
 """
 import json
 import os
 import subprocess
 import sys
-import tempfile
 
 import numpy as np
 import pytest
@@ -150,3 +150,121 @@ def test_reference_files_and_generated_lps_read_the_same(sih, tmp_path):
     ref = _reference_read(paths, str(tmp_path / "ref.npz"))
     for i, path in enumerate(paths):
         _assert_same(sih.read_mps(path), ref, f"{i}/")
+
+
+def _random_mps(rng) -> str:
+    """A seeded random MPS text mixing every record form the readers handle:
+    row kinds (some lower case, repeated, unknown), entries to unknown and to
+    extra N rows, duplicates, odd RHS / RANGES token counts, every bound type,
+    value-less bounds, number forms, tabs, CRLF endings, comments, unknown
+    headers and integer markers."""
+    nr, nc = int(rng.integers(1, 9)), int(rng.integers(1, 9))
+    rows = [f"r{i}" for i in range(nr)]
+    cols = [f"x{j}" for j in range(nc)]
+    num_forms = ["{:.17g}", "{:.3e}", "{:.2f}", "{:.1f}abc", "+{:.4g}"]
+
+    def num():
+        v = float(rng.choice([0.0, 1e-16, 1.0, -2.5, 3.0])) if rng.random() < 0.3 else float(rng.normal(0, 5))
+        s = str(rng.choice(num_forms)).format(v)
+        return s.replace("+-", "-")
+
+    sep = lambda: str(rng.choice([" ", "  ", "\t", "    "]))
+    out = ["* random MPS", f"NAME{sep()}rand{int(rng.integers(1000))}"]
+    if rng.random() < 0.5:
+        out += ["OBJSENSE", f"    {rng.choice(['MAX', 'MIN', 'max', 'MAXIMIZE'])}"]
+    out.append("ROWS")
+    out.append(f" N{sep()}obj")
+    for r in rows:
+        out.append(f" {rng.choice(['E', 'L', 'G', 'e', 'l', 'g'])}{sep()}{r}")
+    if rng.random() < 0.3:
+        out.append(f" N{sep()}obj2")
+    if rng.random() < 0.3:
+        out.append(f" L{sep()}{rows[0]}")  # repeated definition: the first one stays
+    if rng.random() < 0.2:
+        out.append(f" X{sep()}odd")
+    if rng.random() < 0.2:
+        out.append("UNKNOWNSECTION")
+    out.append("COLUMNS")
+    marker = False
+    for j, cname in enumerate(cols):
+        if rng.random() < 0.2:
+            out.append(f"    M{sep()}'MARKER'{sep()}{'INTEND' if marker else 'INTORG'}")
+            marker = not marker
+        targets = ["obj"] + list(rng.choice(rows + ["nowhere", "obj2"], size=int(rng.integers(0, 4))))
+        for t in targets:
+            if rng.random() < 0.5:
+                out.append(f"    {cname}{sep()}{t}{sep()}{num()}")
+            else:
+                t2 = str(rng.choice(rows))
+                out.append(f"    {cname}{sep()}{t}{sep()}{num()}{sep()}{t2}{sep()}{num()}")
+    out.append("RHS")
+    for r in list(rng.choice(rows + ["obj"], size=int(rng.integers(0, nr + 2)))):
+        if rng.random() < 0.5:
+            out.append(f"    rhs{sep()}{r}{sep()}{num()}")
+        else:
+            out.append(f"    {r}{sep()}{num()}")
+    if rng.random() < 0.6:
+        out.append("RANGES")
+        for r in list(rng.choice(rows, size=int(rng.integers(1, nr + 1)))):
+            out.append(f"    rng{sep()}{r}{sep()}{num()}")
+    out.append("BOUNDS")
+    for cname in list(rng.choice(cols + ["newcol"], size=int(rng.integers(0, 2 * nc + 1)))):
+        bt = str(rng.choice(["UP", "LO", "FX", "FR", "MI", "PL", "BV", "UI", "LI", "SC", "up"]))
+        if bt in ("FR", "MI", "PL", "BV") and rng.random() < 0.5:
+            out.append(f" {bt}{sep()}bnd{sep()}{cname}")
+        else:
+            v = abs(float(rng.normal(0, 4))) + (0.0 if bt in ("LO", "LI") else 1.0)
+            out.append(f" {bt}{sep()}bnd{sep()}{cname}{sep()}{v:.6g}")
+    out.append("ENDATA")
+    eol = "\r\n" if rng.random() < 0.3 else "\n"
+    return eol.join(out) + eol
+
+
+@pytest.mark.skipif(not (os.path.isdir(REF_CORE) and any(f.startswith("_core") for f in os.listdir(REF_CORE))),
+                    reason="reference build (oracle/ref_build.sh) not present")
+def test_random_mps_texts_read_like_the_reference(sih, tmp_path):
+    """200 seeded random MPS texts: wherever the reference reader returns a
+    problem this reader returns the same arrays; wherever it raises, this one
+    reports an error."""
+    rng = np.random.default_rng(20261204)
+    paths = []
+    for k in range(200):
+        path = tmp_path / f"r{k}.mps"
+        path.write_bytes(_random_mps(rng).encode())
+        paths.append(str(path))
+    code = ("import sys, json, numpy as np\n"
+            f"sys.path.insert(0, {REF_CORE!r})\n"
+            "import _core\n"
+            "arr, ok = {}, []\n"
+            f"for i, path in enumerate({paths!r}):\n"
+            "    try:\n"
+            "        r = _core.read_mps(path)\n"
+            "    except Exception:\n"
+            "        ok.append(False); continue\n"
+            "    ok.append(True); A = r.A\n"
+            "    for k in ('csc_col_ptr', 'csc_row_ind', 'csc_values'):\n"
+            "        arr[f'{i}/{k}'] = np.asarray(getattr(A, k)())\n"
+            "    for k in ('c', 'col_lower', 'col_upper', 'row_lower', 'row_upper'):\n"
+            "        arr[f'{i}/{k}'] = np.asarray(getattr(r, k), dtype=np.float64)\n"
+            "    arr[f'{i}/sense'] = np.int64(int(r.sense)); arr[f'{i}/obj_offset'] = np.float64(r.obj_offset)\n"
+            "    arr[f'{i}/integer_columns'] = np.int64(sum(int(t) != 0 for t in r.var_types))\n"
+            f"np.savez({str(tmp_path / 'ref.npz')!r}, **arr)\n"
+            "print(json.dumps(ok))\n")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    ok = json.loads(r.stdout.strip().splitlines()[-1])
+    ref = np.load(tmp_path / "ref.npz")
+    reads = 0
+    for i, path in enumerate(paths):
+        if not ok[i]:
+            with pytest.raises(sih.SihPdhgError):
+                sih.read_mps(path)
+            continue
+        p = sih.read_mps(path)
+        reads += 1
+        for k in ("csc_col_ptr", "csc_row_ind", "csc_values", "c", "col_lower", "col_upper", "row_lower",
+                  "row_upper"):
+            np.testing.assert_array_equal(_arrays(p)[k], ref[f"{i}/{k}"], err_msg=f"{path}: {k}")
+        assert int(p.sense) == int(ref[f"{i}/sense"]) and float(p.obj_offset) == float(ref[f"{i}/obj_offset"])
+        assert p.integer_columns == int(ref[f"{i}/integer_columns"])
+    assert reads >= 50  # most texts are valid problems
