@@ -39,6 +39,7 @@
 #include <limits>
 #include <string>
 #include <string_view>
+#include <thread>
 #include <vector>
 
 #include "sih_pdhg.h"
@@ -75,6 +76,21 @@ std::string upper(std::string_view s) {
     std::string out(s);
     for (auto& ch : out) ch = (char)std::toupper(static_cast<unsigned char>(ch));
     return out;
+}
+
+// Section of a header keyword, or Sec::None for a header line the reader skips.
+Sec header_section(std::string_view first_token) {
+    const std::string h = upper(first_token);
+    if (h == "NAME") return Sec::Name;
+    if (h == "OBJSENSE") return Sec::ObjSense;
+    if (h == "ROWS") return Sec::Rows;
+    if (h == "COLUMNS") return Sec::Columns;
+    if (h == "RHS") return Sec::Rhs;
+    if (h == "RANGES") return Sec::Ranges;
+    if (h == "BOUNDS") return Sec::Bounds;
+    if (h == "QUADOBJ" || h == "QMATRIX") return Sec::Quad;
+    if (h == "ENDATA") return Sec::End;
+    return Sec::None;
 }
 
 // White-space separated tokens; apostrophes toggle quoting and stay in the token.
@@ -122,7 +138,13 @@ bool plain_decimal(std::string_view t) {
     return i == n;
 }
 
-double number(std::string_view t, int64_t line_no) {
+// A token that std::stod would reject (nothing converts, or out of range).
+struct NumberError {
+    std::string token;
+    bool out_of_range;
+};
+
+double number_value(std::string_view t) {
     if (plain_decimal(t)) {
         double v = 0.0;
         const auto r = std::from_chars(t.data(), t.data() + t.size(), v);
@@ -143,11 +165,22 @@ double number(std::string_view t, int64_t line_no) {
     char* end = nullptr;
     errno = 0;
     const double v = std::strtod(s, &end);
-    if (end == s)
-        throw ParseError{"line " + std::to_string(line_no) + ": '" + std::string(t) + "' is not a number"};
-    if (errno == ERANGE)
-        throw ParseError{"line " + std::to_string(line_no) + ": '" + std::string(t) + "' is out of range"};
+    if (end == s) throw NumberError{std::string(t), false};
+    if (errno == ERANGE) throw NumberError{std::string(t), true};
     return v;
+}
+
+std::string number_message(int64_t line_no, const NumberError& e) {
+    return "line " + std::to_string(line_no) + ": '" + e.token + (e.out_of_range ? "' is out of range"
+                                                                                  : "' is not a number");
+}
+
+double number(std::string_view t, int64_t line_no) {
+    try {
+        return number_value(t);
+    } catch (const NumberError& e) {
+        throw ParseError{number_message(line_no, e)};
+    }
 }
 
 struct RowDef {
@@ -212,6 +245,17 @@ class NameTable {
     }
 };
 
+// COLUMNS bodies of at least this many bytes are parsed on several threads
+// (environment SIH_PDHG_MPS_PARALLEL_BYTES overrides; 0 = always).
+size_t parallel_min_bytes() {
+    if (const char* v = std::getenv("SIH_PDHG_MPS_PARALLEL_BYTES")) {
+        char* end = nullptr;
+        const long long n = std::strtoll(v, &end, 10);
+        if (end != v && n >= 0) return (size_t)n;
+    }
+    return (size_t)8 << 20;
+}
+
 struct Reader {
     sih_pdhg_mps& P;
     NameTable row_index;
@@ -229,20 +273,165 @@ struct Reader {
 
     explicit Reader(sih_pdhg_mps& p) : P(p) {}
 
+    // A new column as the reference creates one: c 0, bounds [0, +inf).
+    int64_t create_column(std::string_view name, bool integer) {
+        const int64_t idx = (int64_t)P.c.size();
+        cols.insert(name, idx);
+        col_int.push_back(integer ? 1 : 0);
+        P.col_lower.push_back(0.0);
+        P.col_upper.push_back(kInf);
+        P.c.push_back(0.0);
+        return idx;
+    }
+
     int64_t column(std::string_view name) {
         if (last_col_idx >= 0 && name == last_col) return last_col_idx;
         int64_t idx = cols.find(name);
-        if (idx < 0) {
-            idx = (int64_t)P.c.size();
-            cols.insert(name, idx);
-            col_int.push_back(integer_marker ? 1 : 0);
-            P.col_lower.push_back(0.0);
-            P.col_upper.push_back(kInf);
-            P.c.push_back(0.0);
-        }
+        if (idx < 0) idx = create_column(name, integer_marker);
         last_col = name;
         last_col_idx = idx;
         return idx;
+    }
+
+    // End of the COLUMNS body that starts at `pos`: the start of the next line
+    // with a section keyword (other header lines are skipped and stay inside).
+    static size_t columns_end(std::string_view text, size_t pos) {
+        std::vector<std::string_view> tok;
+        while (pos < text.size()) {
+            size_t eol = text.find('\n', pos);
+            if (eol == std::string_view::npos) eol = text.size();
+            const std::string_view line = text.substr(pos, eol - pos);
+            if (!line.empty() && line[0] != '*' && !is_space(line[0]) && tokenize(line, tok) > 0 &&
+                header_section(tok[0]) != Sec::None)
+                return pos;
+            pos = eol + 1;
+        }
+        return text.size();
+    }
+
+    // One slice of a COLUMNS body, parsed on its own thread: columns first seen
+    // here (with the integer marker state at that point, -1 = the state the
+    // slice starts with), entries and objective terms by local column, in file
+    // order, and the slice's first number error.
+    struct ColSlice {
+        NameTable local;
+        std::vector<std::string_view> names;
+        std::vector<signed char> name_marker;
+        std::vector<int32_t> e_lcol, obj_lcol;
+        std::vector<int64_t> e_row;
+        std::vector<double> e_val, obj_val;
+        signed char final_marker = -1;
+        bool failed = false;
+        size_t fail_line = 0;  // byte offset of the failing line
+        NumberError error{std::string(), false};
+    };
+
+    void parse_slice(std::string_view text, size_t b, size_t e, ColSlice& S) const {
+        std::vector<std::string_view> tok;
+        tok.reserve(16);
+        signed char marker = -1;
+        std::string_view last;
+        int32_t last_id = -1;
+        size_t pos = b;
+        while (pos < e) {
+            size_t eol = text.find('\n', pos);
+            if (eol == std::string_view::npos || eol > e) eol = e;
+            const std::string_view line = text.substr(pos, eol - pos);
+            const size_t line_start = pos;
+            pos = eol + 1;
+            if (line.empty() || line[0] == '*' || !is_space(line[0])) continue;  // comment, skipped header
+            const int nt = tokenize(line, tok);
+            if (nt >= 3 && (tok[1] == "'MARKER'" || tok[1] == "MARKER")) {
+                const std::string mk = upper(tok[2]);
+                if (mk == "'INTORG'" || mk == "INTORG") marker = 1;
+                else if (mk == "'INTEND'" || mk == "INTEND") marker = 0;
+                continue;
+            }
+            if (nt < 3) continue;
+            int32_t id = last_id;
+            if (id < 0 || tok[0] != last) {
+                int64_t f = S.local.find(tok[0]);
+                if (f < 0) {
+                    f = (int64_t)S.names.size();
+                    S.local.insert(tok[0], f);
+                    S.names.push_back(tok[0]);
+                    S.name_marker.push_back(marker);
+                }
+                id = (int32_t)f;
+                last = tok[0];
+                last_id = id;
+            }
+            for (int k = 1; k + 1 < nt; k += 2) {
+                double v;
+                try {
+                    v = number_value(tok[k + 1]);
+                } catch (const NumberError& err) {
+                    S.failed = true;
+                    S.fail_line = line_start;
+                    S.error = err;
+                    return;
+                }
+                if (have_obj && tok[k] == obj_row) {
+                    S.obj_lcol.push_back(id);
+                    S.obj_val.push_back(v);
+                } else {
+                    const int64_t i = row_index.find(tok[k]);
+                    if (i >= 0) {
+                        S.e_lcol.push_back(id);
+                        S.e_row.push_back(i);
+                        S.e_val.push_back(v);
+                    }
+                }
+            }
+        }
+        S.final_marker = marker;
+    }
+
+    // The COLUMNS body [b, e) on several threads, merged in file order: the
+    // same columns (first appearance order, marker state), entries and
+    // objective sums as a sequential pass, and the first number error of the
+    // file.  `line_no` is the number of the COLUMNS header line.
+    void parse_columns_parallel(std::string_view text, size_t b, size_t e, int64_t line_no) {
+        int T = (int)std::thread::hardware_concurrency();
+        T = std::max(2, std::min(T, 32));
+        std::vector<size_t> cut(T + 1, b);
+        cut[T] = e;
+        for (int k = 1; k < T; ++k) {
+            size_t q = b + (size_t)((double)(e - b) * k / T);
+            if (q > b) {
+                const size_t nl = text.find('\n', q - 1);
+                q = (nl == std::string_view::npos || nl + 1 > e) ? e : nl + 1;
+            }
+            cut[k] = std::max(cut[k - 1], std::min(q, e));
+        }
+        std::vector<ColSlice> slices(T);
+        std::vector<std::thread> pool;
+        for (int k = 0; k < T; ++k)
+            pool.emplace_back([&, k] { parse_slice(text, cut[k], cut[k + 1], slices[k]); });
+        for (auto& t : pool) t.join();
+        for (const ColSlice& S : slices)
+            if (S.failed) {
+                const int64_t line = line_no + 1 + std::count(text.begin() + b, text.begin() + S.fail_line, '\n');
+                throw ParseError{number_message(line, S.error)};
+            }
+        bool state = integer_marker;
+        for (const ColSlice& S : slices) {
+            std::vector<int64_t> map(S.names.size());
+            for (size_t t = 0; t < S.names.size(); ++t) {
+                int64_t g = cols.find(S.names[t]);
+                if (g < 0) g = create_column(S.names[t], S.name_marker[t] >= 0 ? S.name_marker[t] == 1 : state);
+                map[t] = g;
+            }
+            if (S.final_marker >= 0) state = S.final_marker == 1;
+            for (size_t q = 0; q < S.obj_lcol.size(); ++q) P.c[map[S.obj_lcol[q]]] += S.obj_val[q];
+            for (size_t q = 0; q < S.e_lcol.size(); ++q) {
+                e_row.push_back(S.e_row[q]);
+                e_col.push_back(map[S.e_lcol[q]]);
+                e_val.push_back(S.e_val[q]);
+            }
+        }
+        integer_marker = state;
+        last_col_idx = -1;
     }
 
     void parse(std::string_view text) {
@@ -260,26 +449,18 @@ struct Reader {
             if (line.empty() || line[0] == '*') continue;
             if (!is_space(line[0])) {
                 if (tokenize(line, tok) == 0) continue;
-                const std::string h = upper(tok[0]);
-                if (h == "NAME") {
-                    sec = Sec::Name;
-                    if (tok.size() > 1) P.name.assign(tok[1]);
-                } else if (h == "OBJSENSE") {
-                    sec = Sec::ObjSense;
-                } else if (h == "ROWS") {
-                    sec = Sec::Rows;
-                } else if (h == "COLUMNS") {
-                    sec = Sec::Columns;
-                } else if (h == "RHS") {
-                    sec = Sec::Rhs;
-                } else if (h == "RANGES") {
-                    sec = Sec::Ranges;
-                } else if (h == "BOUNDS") {
-                    sec = Sec::Bounds;
-                } else if (h == "QUADOBJ" || h == "QMATRIX") {
-                    sec = Sec::Quad;
-                } else if (h == "ENDATA") {
-                    return;
+                const Sec h = header_section(tok[0]);
+                if (h == Sec::None) continue;  // a header the reference skips: the section stays
+                if (h == Sec::End) return;
+                sec = h;
+                if (h == Sec::Name && tok.size() > 1) P.name.assign(tok[1]);
+                if (h == Sec::Columns) {
+                    const size_t body_end = columns_end(text, pos);
+                    if (body_end - std::min(pos, body_end) >= parallel_min_bytes()) {
+                        parse_columns_parallel(text, pos, body_end, line_no);
+                        line_no += std::count(text.begin() + pos, text.begin() + body_end, '\n');
+                        pos = body_end;
+                    }
                 }
                 continue;
             }

@@ -268,3 +268,32 @@ def test_random_mps_texts_read_like_the_reference(sih, tmp_path):
         assert int(p.sense) == int(ref[f"{i}/sense"]) and float(p.obj_offset) == float(ref[f"{i}/obj_offset"])
         assert p.integer_columns == int(ref[f"{i}/integer_columns"])
     assert reads >= 50  # most texts are valid problems
+
+
+def test_sliced_columns_parse_equals_the_sequential_parse(sih, monkeypatch):
+    """COLUMNS bodies cut into per-thread slices (forced here for small texts)
+    give the same problem and the same error messages as the one-thread pass."""
+    rng = np.random.default_rng(7)
+    texts = [_random_mps(rng) for _ in range(60)]
+    texts += [open(os.path.join(MPS_DIR, f)).read() for f in sorted(os.listdir(MPS_DIR)) if f.endswith(".mps")]
+
+    def read_all():
+        out = []
+        for t in texts:
+            try:
+                out.append(("ok", _arrays(sih.read_mps_text(t))))
+            except sih.SihPdhgError as e:
+                out.append(("err", str(e)))
+        return out
+
+    monkeypatch.setenv("SIH_PDHG_MPS_PARALLEL_BYTES", str(1 << 40))
+    seq = read_all()
+    monkeypatch.setenv("SIH_PDHG_MPS_PARALLEL_BYTES", "0")
+    par = read_all()
+    for (ka, a), (kb, b) in zip(seq, par):
+        assert ka == kb
+        if ka == "err":
+            assert a == b
+        else:
+            for k in ARRAYS:
+                np.testing.assert_array_equal(a[k], b[k])
