@@ -703,6 +703,12 @@ int sih_pdhg_read_mps(const char* path, sih_pdhg_mps** out) {
     char buf[1 << 16];
     size_t got;
     try {
+        // one allocation of the file's size when it can be known, then read to the end
+        if (std::fseek(f, 0, SEEK_END) == 0) {
+            const long size = std::ftell(f);
+            if (size > 0) text.reserve((size_t)size);
+            std::rewind(f);
+        }
         while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, got);
     } catch (const std::bad_alloc&) {
         std::fclose(f);
