@@ -42,6 +42,8 @@
 #include <thread>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "sih_pdhg.h"
 
 namespace sihg {
@@ -670,6 +672,10 @@ int read_text(std::string_view text, sih_pdhg_mps** out) {
         delete P;
         sihg::set_last_error("MPS: out of host memory");
         return SIH_PDHG_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {  // nothing may cross the C boundary
+        delete P;
+        sihg::set_last_error(std::string("MPS: ") + e.what());
+        return SIH_PDHG_ERR_INVALID_ARGUMENT;
     }
     *out = P;
     return SIH_PDHG_OK;
@@ -703,14 +709,18 @@ int sih_pdhg_read_mps(const char* path, sih_pdhg_mps** out) {
     char buf[1 << 16];
     size_t got;
     try {
-        // one allocation of the file's size when it can be known, then read to the end
-        if (std::fseek(f, 0, SEEK_END) == 0) {
-            const long size = std::ftell(f);
-            if (size > 0) text.reserve((size_t)size);
-            std::rewind(f);
+        // a directory is an error; a regular file is read into one allocation of
+        // its size; anything else (a pipe, a device) is read to its end
+        struct stat st;
+        const bool have_stat = fstat(fileno(f), &st) == 0;
+        if (have_stat && S_ISDIR(st.st_mode)) {
+            std::fclose(f);
+            sihg::set_last_error(std::string("is a directory: ") + path);
+            return SIH_PDHG_ERR_INVALID_ARGUMENT;
         }
+        if (have_stat && S_ISREG(st.st_mode) && st.st_size > 0) text.reserve((size_t)st.st_size);
         while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, got);
-    } catch (const std::bad_alloc&) {
+    } catch (const std::exception&) {
         std::fclose(f);
         sihg::set_last_error("MPS: out of host memory");
         return SIH_PDHG_ERR_OUT_OF_MEMORY;

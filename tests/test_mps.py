@@ -89,6 +89,11 @@ def test_text_equals_file_and_missing_file_is_an_error(sih):
     with pytest.raises(sih.SihPdhgError) as e:
         sih.read_mps(os.path.join(MPS_DIR, "no_such_file.mps"))
     assert e.value.code == 1
+    with pytest.raises(sih.SihPdhgError) as e:  # a directory: an error, not a crash
+        sih.read_mps(MPS_DIR)
+    assert e.value.code == 1 and "directory" in str(e.value)
+    empty = sih.read_mps_text(b"")  # no records: the empty problem, as the reference reads it
+    assert empty.num_rows() == 0 and empty.num_cols() == 0 and empty.name == "problem"
 
 
 def _generated():
