@@ -520,7 +520,7 @@ static int resolve_adjoint_options(const sih_pdhg_adjoint_options* in, sih_pdhg_
     return SIH_PDHG_OK;
 }
 
-extern "C" int sih_pdhg_adjoint_batch(const sih_pdhg_problem* problems, int32_t count, const double* const* x,
+static int adjoint_batch_impl(const sih_pdhg_problem* problems, int32_t count, const double* const* x,
                                       const double* const* row_duals, const double* const* grad_x,
                                       double* const* grad_c, double* const* grad_row_lower,
                                       double* const* grad_row_upper, double* const* grad_col_lower,
@@ -583,7 +583,19 @@ extern "C" int sih_pdhg_adjoint_batch(const sih_pdhg_problem* problems, int32_t 
     return SIH_PDHG_OK;
 }
 
-extern "C" int sih_pdhg_polish_batch(const sih_pdhg_problem* problems, int32_t count, const double* const* x,
+extern "C" int sih_pdhg_adjoint_batch(const sih_pdhg_problem* problems, int32_t count, const double* const* x,
+                                      const double* const* row_duals, const double* const* grad_x,
+                                      double* const* grad_c, double* const* grad_row_lower,
+                                      double* const* grad_row_upper, double* const* grad_col_lower,
+                                      double* const* grad_col_upper, const sih_pdhg_adjoint_options* opts,
+                                      sih_pdhg_adjoint_info* info) {
+    return guarded([&] {
+        return adjoint_batch_impl(problems, count, x, row_duals, grad_x, grad_c, grad_row_lower, grad_row_upper,
+                                  grad_col_lower, grad_col_upper, opts, info);
+    });
+}
+
+static int polish_batch_impl(const sih_pdhg_problem* problems, int32_t count, const double* const* x,
                                      const double* const* row_duals, double* const* x_out,
                                      double* const* row_duals_out, const sih_pdhg_adjoint_options* opts,
                                      sih_pdhg_polish_info* info) {
@@ -694,4 +706,11 @@ extern "C" int sih_pdhg_polish_batch(const sih_pdhg_problem* problems, int32_t c
         }
     });
     return SIH_PDHG_OK;
+}
+
+extern "C" int sih_pdhg_polish_batch(const sih_pdhg_problem* problems, int32_t count, const double* const* x,
+                                     const double* const* row_duals, double* const* x_out,
+                                     double* const* row_duals_out, const sih_pdhg_adjoint_options* opts,
+                                     sih_pdhg_polish_info* info) {
+    return guarded([&] { return polish_batch_impl(problems, count, x, row_duals, x_out, row_duals_out, opts, info); });
 }

@@ -181,7 +181,7 @@ int sih_pdhg_get_vram_info(uint64_t* total_bytes, uint64_t* free_bytes, uint64_t
     return SIH_PDHG_OK;
 }
 
-int sih_pdhg_solve_ex(const sih_pdhg_problem* problem, const sih_pdhg_config* config, const sih_pdhg_options* opts_in,
+static int solve_ex_impl(const sih_pdhg_problem* problem, const sih_pdhg_config* config, const sih_pdhg_options* opts_in,
                       sih_pdhg_result* result) {
     const auto t0 = std::chrono::steady_clock::now();
     if (!result) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "result is NULL");
@@ -205,6 +205,11 @@ int sih_pdhg_solve_ex(const sih_pdhg_problem* problem, const sih_pdhg_config* co
                                                    : solve_mixed(hp, *config, opts, result);
     result->time_wall_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return rc;
+}
+
+int sih_pdhg_solve_ex(const sih_pdhg_problem* problem, const sih_pdhg_config* config, const sih_pdhg_options* opts_in,
+                      sih_pdhg_result* result) {
+    return guarded([&] { return solve_ex_impl(problem, config, opts_in, result); });
 }
 
 int sih_pdhg_solve(const sih_pdhg_problem* problem, const sih_pdhg_config* config, sih_pdhg_result* result) {

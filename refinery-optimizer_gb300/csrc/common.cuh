@@ -8,6 +8,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -26,6 +28,20 @@ struct Status {
 inline int fail(int code, const std::string& msg) {
     set_last_error(msg);
     return code;
+}
+
+// Runs an entry point's body so that no C++ exception crosses the C ABI:
+// std::bad_alloc becomes SIH_PDHG_ERR_OUT_OF_MEMORY, any other exception
+// SIH_PDHG_ERR_INVALID_ARGUMENT with its message.
+template <class F>
+int guarded(F&& body) {
+    try {
+        return body();
+    } catch (const std::bad_alloc&) {
+        return fail(SIH_PDHG_ERR_OUT_OF_MEMORY, "out of host memory");
+    } catch (const std::exception& e) {
+        return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, std::string("unexpected error: ") + e.what());
+    }
 }
 
 inline int cuda_fail(cudaError_t e, const char* what, const char* file, int line) {

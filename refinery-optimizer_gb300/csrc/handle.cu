@@ -37,7 +37,7 @@ uint64_t mixed_h2d_bytes(const HostProblem& p) { return instance_h2d_bytes(p) + 
 
 extern "C" {
 
-int sih_pdhg_create(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
+static int create_impl(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
                     const sih_pdhg_options* opts_in, sih_pdhg_handle** out) {
     if (!out) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "out is NULL");
     *out = nullptr;
@@ -72,7 +72,12 @@ int sih_pdhg_create(const sih_pdhg_problem* problems, int32_t count, const sih_p
     return SIH_PDHG_OK;
 }
 
-int sih_pdhg_run(sih_pdhg_handle* h, double* device_seconds) {
+int sih_pdhg_create(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
+                    const sih_pdhg_options* opts_in, sih_pdhg_handle** out) {
+    return guarded([&] { return create_impl(problems, count, config, opts_in, out); });
+}
+
+static int run_impl(sih_pdhg_handle* h, double* device_seconds) {
     if (!h) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "handle is NULL");
     double secs = 0.0;
     if (h->mixed) {
@@ -89,7 +94,11 @@ int sih_pdhg_run(sih_pdhg_handle* h, double* device_seconds) {
     return SIH_PDHG_OK;
 }
 
-int sih_pdhg_get_result(sih_pdhg_handle* h, int32_t index, sih_pdhg_result* r) {
+int sih_pdhg_run(sih_pdhg_handle* h, double* device_seconds) {
+    return guarded([&] { return run_impl(h, device_seconds); });
+}
+
+static int get_result_impl(sih_pdhg_handle* h, int32_t index, sih_pdhg_result* r) {
     if (!h || !r) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "NULL handle or result");
     if (index < 0 || index >= (int32_t)h->hps.size()) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "index out of range");
     if (!h->ran) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "sih_pdhg_run has not been called");
@@ -108,17 +117,30 @@ int sih_pdhg_get_result(sih_pdhg_handle* h, int32_t index, sih_pdhg_result* r) {
     return SIH_PDHG_OK;
 }
 
-int sih_pdhg_time_kernels(sih_pdhg_handle* h, int32_t reps, double* seconds, double* bytes) {
+int sih_pdhg_get_result(sih_pdhg_handle* h, int32_t index, sih_pdhg_result* r) {
+    return guarded([&] { return get_result_impl(h, index, r); });
+}
+
+static int time_kernels_impl(sih_pdhg_handle* h, int32_t reps, double* seconds, double* bytes) {
     if (!h || !seconds || reps < 1) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "bad arguments");
     if (!h->mixed) return fail(SIH_PDHG_ERR_UNSUPPORTED, "kernel timing is available for the mixed algorithm");
     return h->mixed->time_kernels(reps, seconds, bytes);
 }
 
-int sih_pdhg_set_start(sih_pdhg_handle* h, int32_t index, const double* x, const double* row_duals,
+int sih_pdhg_time_kernels(sih_pdhg_handle* h, int32_t reps, double* seconds, double* bytes) {
+    return guarded([&] { return time_kernels_impl(h, reps, seconds, bytes); });
+}
+
+static int set_start_impl(sih_pdhg_handle* h, int32_t index, const double* x, const double* row_duals,
                        double primal_weight) {
     if (!h) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "NULL handle");
     if (!h->mixed) return fail(SIH_PDHG_ERR_UNSUPPORTED, "warm starts are available for the mixed algorithm");
     return h->mixed->set_start(index, x, row_duals, primal_weight);
+}
+
+int sih_pdhg_set_start(sih_pdhg_handle* h, int32_t index, const double* x, const double* row_duals,
+                       double primal_weight) {
+    return guarded([&] { return set_start_impl(h, index, x, row_duals, primal_weight); });
 }
 
 int sih_pdhg_get_task_nnz(const sih_pdhg_handle* h, int32_t* task_nnz) {
@@ -130,7 +152,7 @@ int sih_pdhg_get_task_nnz(const sih_pdhg_handle* h, int32_t* task_nnz) {
 
 void sih_pdhg_destroy(sih_pdhg_handle* h) { delete h; }
 
-int sih_pdhg_solve_batch(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
+static int solve_batch_impl(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
                          const sih_pdhg_options* opts, sih_pdhg_result* results) {
     if (!results) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "results is NULL");
     sih_pdhg_handle* h = nullptr;
@@ -143,6 +165,11 @@ int sih_pdhg_solve_batch(const sih_pdhg_problem* problems, int32_t count, const 
         results[b].time_solver_sec = secs;
     }
     return SIH_PDHG_OK;
+}
+
+int sih_pdhg_solve_batch(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
+                         const sih_pdhg_options* opts, sih_pdhg_result* results) {
+    return guarded([&] { return solve_batch_impl(problems, count, config, opts, results); });
 }
 
 }  // extern "C"
