@@ -29,9 +29,11 @@ Workloads (seeded synthetic LPs, FP64 data, generators in sih_pdhg.generators):
 Multi-GPU: replicas (each rank solves its own copy of a single LP, or its own
 seeded batch of a batch workload; no data-path exchange; scaling "weak").
 --impl reference times the reference's algorithm (plain FP32 PDHG) through its
-CPU port (oracle/pdhg_oracle.c, OpenMP over all host threads) on a bounded
-sample of iterations, scaled by the iterations that algorithm needs to reach
-the same tolerance on the same LP.
+CPU port (oracle/pdhg_oracle.c, OpenMP over all host threads): every timed
+step is one complete solve of the workload LP from the initial point until the
+FP64 relative KKT of its iterate is <= the tolerance (checked every 100
+iterations); warm-up steps run 200 iterations each (page-in, thread start).
+Batch workloads time the first scenario's complete solve and scale by nonzeros.
 """
 from __future__ import annotations
 
@@ -51,23 +53,17 @@ sys.path.insert(0, PKG)
 
 METRIC = "time-to-1e-4 rel. KKT & HBM GB/s: batched mixed vs plain PDHG, 1×GB300"
 
-# Iterations the plain reference algorithm (FP32 PDHG, fixed diagonal steps,
-# gpu_solver.cpp:128-151) needs on each workload before its best iterate and
-# last dual reach relative KKT <= 1e-4: the first point of a measured grid at
-# or below the tolerance (this engine's plain path, same iterates as the
-# reference up to FP32 summation order).  zipf-500kx1m: 14,000 iterations give
-# a relative gap of 1.007e-4, 16,000 give 8.3e-5; random-2kx5k: 8,000 give
-# 1.08e-4, 12,000 give 5.3e-5.
-PLAIN_ITERS_TO_TOL = {
-    "zipf-500kx1m": 16000,
-    "random-2kx5k": 12000,
-}
-PLAIN_ITERS_LOWER_BOUND = {
-    "zipf-500kx1m": 200000,
-    "random-2kx5k": 20000,
-    "refinery-168p": 100000,
-    "refinery-512": 100000,
-    "refinery-64": 100000,
+# Iteration cap of the plain reference algorithm's solves to tolerance (CPU
+# arm and the plain comparison on the GPU): on the refinery LPs it does not
+# reach 1e-4 within any affordable budget; a capped solve is reported as a
+# lower bound.
+PLAIN_CAP = {
+    "zipf-500kx1m": 200_000,
+    "random-2kx5k": 200_000,
+    "refinery-168p": 100_000,
+    "refinery-512": 100_000,
+    "refinery-64": 100_000,
+    "random-2kx5k-x256": 200_000,
 }
 
 # DRAM bytes per launch of the dominant kernels, read from one ncu capture of
@@ -225,8 +221,9 @@ def measured_hbm_peak():
 
 # ------------------------------------------------------------------ CPU baselines (oracle = test/baseline only)
 def cpu_pdlp_sample(problem, gpu_attempts: int, sample_s: float) -> dict:
-    """FP64 CPU port of the same mixed algorithm (oracle/pdlp_oracle.c, one
-    thread) on a bounded number of steps, scaled to the GPU's step count."""
+    """FP64 CPU port of the same mixed algorithm (oracle/pdlp_oracle.c: its
+    SpMVs and elementwise passes on every host thread, as the reference arm
+    uses them) on a bounded number of steps, scaled to the GPU's step count."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
 
@@ -241,7 +238,7 @@ def cpu_pdlp_sample(problem, gpu_attempts: int, sample_s: float) -> dict:
         oracle.pdlp_solve(problem, max_attempts=attempts, tol=1e-30)
         dt = time.perf_counter() - t0
     per_step = dt / attempts  # includes scaling and evaluations, amortised
-    return {"value": per_step * gpu_attempts, "unit": "s", "cores": 1, "kind": "port",
+    return {"value": per_step * gpu_attempts, "unit": "s", "cores": os.cpu_count() or 1, "kind": "port",
             "sample": f"{attempts} steps of the FP64 CPU port of the same algorithm ({dt:.1f} s), "
                       f"scaled to the {gpu_attempts} steps the GPU needed"}
 
@@ -258,14 +255,30 @@ def cpu_plain_per_iteration(data, iters: int, threads: int) -> float:
     return (time.perf_counter() - t0) / iters
 
 
+# ------------------------------------------------------------------ shared config
+def workload_config(name: str, probs, tol: float) -> dict:
+    """`config` of both arms' lines (same keys and values, so the two lines
+    describe one workload)."""
+    nnz = sum(p.num_nonzeros() for p in probs)
+    cfg = {"workload": name, "m": sum(p.num_rows() for p in probs), "n": sum(p.num_cols() for p in probs),
+           "nnz": nnz, "tol": tol,
+           "l2": "working set larger than the 129 MB L2 (no flush needed)" if nnz * 16 > 129e6
+           else "working set L2-resident (small LP: latency-bound)"}
+    if len(probs) > 1:
+        cfg["instances"] = len(probs)
+    return cfg
+
+
 # ------------------------------------------------------------------ reference arm
 def run_reference(args) -> None:
+    """The reference's algorithm on the host cores: plain FP32 PDHG (its CPU
+    port, oracle/pdhg_oracle.c, OpenMP over every host thread).  Each timed
+    step is one complete solve from the initial point to FP64 relative KKT <=
+    tol (oracle.plain_solve_kkt); a batch workload solves its first scenario
+    and scales by the batch's nonzeros.  A solve that hits PLAIN_CAP makes the
+    value a lower bound (the line says so)."""
     rank, world, _ = dist_env()
     if rank != 0:
-        return
-    if args.workload.startswith("mps:"):
-        print(json.dumps({"impl": "reference", "unavailable": "the iterations the reference algorithm needs on an "
-                          "arbitrary MPS file are not known (they are measured per workload)"}), flush=True)
         return
     work = make_workload(args.workload)
     probs = as_list(work)
@@ -276,32 +289,33 @@ def run_reference(args) -> None:
 
     oracle.build()
     data = oracle.plain_prepare(prob)
-    its_needed = PLAIN_ITERS_TO_TOL.get(args.workload)
-    lower = its_needed is None
-    if lower:
-        its_needed = PLAIN_ITERS_LOWER_BOUND[args.workload]
-    # a batch is timed on its first scenario and scaled by nonzeros
+    cap = PLAIN_CAP.get(args.workload, 200_000)
     nnz_scale = sum(p.num_nonzeros() for p in probs) / prob.num_nonzeros()
-    # each step: a bounded sample of iterations sized to ~2 s
-    probe = cpu_plain_per_iteration(data, 3, threads)
-    sample = max(3, int(2.0 / max(probe, 1e-6)))
-    for _ in range(args.warmup):
-        cpu_plain_per_iteration(data, max(3, sample // 4), threads)
-    ests = []
+    for _ in range(args.warmup):  # short: page-in and thread start, not a solve
+        oracle.plain_iterations(data, 200, threads)
+    times, results = [], []
+    t_wall = time.perf_counter()
     for _ in range(args.steps):
-        ests.append(cpu_plain_per_iteration(data, sample, threads) * its_needed * nnz_scale)
-    value = statistics.mean(ests)
-    note = (f"{sample} iterations of the reference algorithm's CPU port per step, x {its_needed} iterations "
-            + ("(lower bound: the plain algorithm did not reach the tolerance within this many)" if lower else
-               "needed to reach the tolerance"))
+        t0 = time.perf_counter()
+        r = oracle.plain_solve_kkt(data, args.tol, eval_every=100, max_iters=cap, threads=threads)
+        times.append((time.perf_counter() - t0) * nnz_scale)
+        results.append(r)
+    wall = time.perf_counter() - t_wall
+    value = statistics.mean(times)
+    its = results[-1]["iterations"]
+    reached = all(max(r["rel_primal"], r["rel_dual"], r["rel_gap"]) <= args.tol for r in results)
+    note = (f"each step one complete solve of the reference algorithm's CPU port ({threads} threads) from its "
+            f"initial point to FP64 relative KKT <= {args.tol:g} (checked every 100 iterations): "
+            f"{its} iterations" + ("" if reached else f" (cap {cap} hit: a lower bound)"))
     if len(probs) > 1:
-        note += f"; timed on scenario 0, x {nnz_scale:.1f} by nonzeros for all {len(probs)} scenarios"
+        note += f"; scenario 0 solved, x {nnz_scale:.1f} by nonzeros for all {len(probs)} scenarios"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, seed 0)",
-            "config": {"workload": args.workload, "m": sum(p.num_rows() for p in probs),
-                       "n": sum(p.num_cols() for p in probs), "nnz": sum(p.num_nonzeros() for p in probs),
-                       "tol": args.tol, "algorithm": "plain FP32 PDHG (reference)"},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, seed 0)",
+            "config": workload_config(args.workload, probs, args.tol),
+            "algorithm": "plain FP32 PDHG (reference), CPU port", "iterations": its,
+            "rel_kkt": [results[-1]["rel_primal"], results[-1]["rel_dual"], results[-1]["rel_gap"]],
+            "reached_tol": reached, "wall_s_per_step": wall / args.steps,
             "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port", "sample": note},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -380,16 +394,7 @@ def run_gb300(args) -> None:
 
     if rank != 0:
         return
-    m = sum(p.num_rows() for p in probs)
-    n = sum(p.num_cols() for p in probs)
-    nnz = sum(p.num_nonzeros() for p in probs)
-    plain_its = PLAIN_ITERS_TO_TOL.get(args.workload)
-    cfg_desc = {"workload": args.workload, "m": m, "n": n, "nnz": nnz, "tol": tol,
-                "algorithm": "mixed-precision restarted adaptive PDHG", "parallelism": f"replicas x{world}",
-                "l2": "working set larger than the 129 MB L2 (no flush needed)" if nnz * 16 > 129e6
-                else "working set L2-resident (small LP: latency-bound)"}
-    if batch:
-        cfg_desc["instances"] = len(probs)
+    cfg_desc = workload_config(args.workload, probs, tol)
     line = {
         "metric": METRIC, "value": step, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": False, "scaling": "weak",
@@ -397,6 +402,7 @@ def run_gb300(args) -> None:
         "data": (f"MPS file {args.workload[4:]}" if args.workload.startswith("mps:")
                  else "synthetic (seeded generator, seed 0)"),
         "config": cfg_desc,
+        "algorithm": "mixed-precision restarted adaptive PDHG", "parallelism": f"replicas x{world}",
         "iterations": max(iters), "restarts": sols[0].restarts,
         "status": max(int(s.status) for s in sols),
         "rel_kkt": [max(s.rel_primal for s in sols), max(s.rel_dual for s in sols), max(s.rel_gap for s in sols)],
@@ -408,10 +414,9 @@ def run_gb300(args) -> None:
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_src,
                      "traffic": NCU_TRAFFIC_PER_LAUNCH.get((args.workload, names[dom])),
                      "algorithmic_bytes_per_launch": byts[dom], "all_kernels_gbs": all_gbs},
-        "plain_reference_iterations_to_tol": plain_its,
     }
-    if not batch and plain_its:
-        line["plain_gpu"] = plain_gpu_time(probs[0], plain_its)
+    if not batch:
+        line["plain_gpu"] = plain_gpu_time(probs[0], tol, PLAIN_CAP.get(args.workload, 200_000))
     if not batch:
         line["cusparse_yardstick"] = cusparse_yardstick(probs[0])
     if batch:
@@ -467,19 +472,44 @@ def cusparse_yardstick(prob, reps: int = 20) -> dict:
     return out
 
 
-def plain_gpu_time(prob, its_needed: int, sample_its: int = 2000) -> dict:
-    """The reference algorithm (plain FP32 PDHG) on this GPU: device seconds per
-    iteration from a bounded run (its own termination test disabled by zero
-    tolerances), times the iterations it needs to reach relative KKT <= 1e-4
-    on this LP (PLAIN_ITERS_TO_TOL)."""
+def plain_gpu_time(prob, tol: float, cap: int) -> dict:
+    """The reference algorithm (plain FP32 PDHG) on this GPU, solved to relative
+    KKT <= tol: runs from the initial point with its own stopping test off
+    (zero tolerances) for 1,000, 2,000, 4,000, ... iterations until one reaches
+    tol, then bisection between the last two to 5 %; `value` is the device
+    time of the shortest run that reached tol (a lower bound when none did
+    within `cap`)."""
     import sih_pdhg
 
-    cfg = sih_pdhg.GpuPdhgConfig(max_iterations=sample_its, tol_primal=0.0, tol_dual=0.0, tol_gap=0.0)
-    sih_pdhg.solve_gpu_pdhg(prob, cfg)  # warm-up
-    sol = sih_pdhg.solve_gpu_pdhg(prob, cfg)
-    per_it = sol.time_solver_sec / sample_its
-    return {"value": per_it * its_needed, "unit": "s", "per_iteration_s": per_it, "iterations_to_tol": its_needed,
-            "sample": f"{sample_its} iterations of the plain path (sih_pdhg_solve) timed on the device"}
+    def run(its):
+        cfg = sih_pdhg.GpuPdhgConfig(max_iterations=its, tol_primal=0.0, tol_dual=0.0, tol_gap=0.0)
+        sol = sih_pdhg.solve_gpu_pdhg(prob, cfg)
+        return max(sol.rel_primal, sol.rel_dual, sol.rel_gap) <= tol, sol.time_solver_sec
+
+    run(1000)  # warm-up
+    lo, hi, hi_t, its = 0, None, None, 1000
+    while True:
+        ok, t = run(its)
+        if ok:
+            hi, hi_t = its, t
+            break
+        lo = its
+        if its >= cap:
+            return {"value": t, "unit": "s", "lower_bound": True, "iterations_to_tol": None,
+                    "sample": f"the plain path (sih_pdhg_solve) did not reach {tol:g} within {cap} iterations "
+                              f"({t:.2f} s device time)"}
+        its = min(cap, its * 2)
+    while hi - lo > max(100, hi // 20):
+        mid = (lo + hi) // 2
+        ok, t = run(mid)
+        if ok:
+            hi, hi_t = mid, t
+        else:
+            lo = mid
+    return {"value": hi_t, "unit": "s", "lower_bound": False, "iterations_to_tol": hi,
+            "per_iteration_s": hi_t / hi,
+            "sample": f"device time of the plain path (sih_pdhg_solve) run for {hi} iterations, the fewest "
+                      f"(to 5 %) whose returned point reaches relative KKT <= {tol:g}"}
 
 
 def plain_sequential_sample(probs, tol: float, count: int, cap: int = 1_000_000) -> dict:

@@ -359,13 +359,17 @@ void sih_pdhg_mps_free(sih_pdhg_mps* mps);
  * max_abs_b and d_out[1] = max column measure / max_abs_c (the reference's
  * norm_p, norm_d), computed by the kernels of sih_pdhg_launch_csr_spmv,
  * _csc_spmv and _residuals, with the working arrays in a file-scope device
- * array of the library instead of cudaMalloc (nothing is allocated, by the
- * library or by CUDA on its behalf).  `nnz` picks the lane groups as the
- * launchers do.
+ * array of the library instead of cudaMalloc: the library calls no
+ * cudaMalloc, cudaFree or allocating routine.  `nnz` picks the lane groups as
+ * the launchers do.  A NaN measure is skipped, as the reference's host loop
+ * skips it.
  * Limit: m + n <= 524,288; larger sizes return SIH_PDHG_ERR_INVALID_ARGUMENT.
  * The array (4 MiB) stays on every GPU that loaded the library until exit.
- * The first call on a device looks the array's address up (once per device,
- * with that device current); make that first call before any stream capture.
+ * The first call on a device does the set-up: it looks the array's address up
+ * with that device current, and CUDA may load the library's device code then
+ * (which is when the array itself is placed); make that first call before any
+ * stream capture.  Later calls allocate nothing.  After cudaDeviceReset the
+ * next call does the set-up again (the context id changed).
  * All calls share the array: calls that overlap on the GPU (other streams,
  * other threads) race and must be serialised by the caller. */
 int sih_pdhg_check_norms_noalloc(int m, int n, int nnz, const int* d_row_ptr, const int* d_col_ind,

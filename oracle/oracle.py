@@ -26,6 +26,15 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+def reference_dir():
+    """Directory of the reference sources as the build recipe oracle/ref_build.sh
+    resolves it (SIH_REFERENCE_DIR or the recipe's default), or None where the
+    sources are absent (the GPU machine)."""
+    out = subprocess.run(["bash", os.path.join(HERE, "ref_build.sh"), "--print-dir"], capture_output=True, text=True)
+    d = out.stdout.strip()
+    return d if out.returncode == 0 and d else None
+
+
 class OracleConfig(C.Structure):
     _fields_ = [("max_iterations", C.c_int32), ("tol_primal", C.c_float), ("tol_dual", C.c_float),
                 ("tol_gap", C.c_float), ("check_frequency", C.c_int32), ("step_tau", C.c_float),
@@ -187,7 +196,10 @@ def plain_prepare(problem):
     rowsum = np.bincount(rows, weights=np.abs(rv), minlength=m).astype(np.float32)
     l, u = f32(problem.col_lower), f32(problem.col_upper)
     x = np.maximum(l, np.minimum(u, np.float32(0)))
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
     return dict(m=m, n=n, cp=cp, ri=ri, cv=cv, rp=rp, ci=ci, rv=rv, c=f32(problem.c), l=l, u=u,
+                cv64=f64(A.csc_values()), rv64=f64(A.csr_values()), c64=f64(problem.c), l64=f64(problem.col_lower),
+                u64=f64(problem.col_upper), rl64=f64(problem.row_lower), ru64=f64(problem.row_upper),
                 rl=f32(problem.row_lower), ru=f32(problem.row_upper),
                 tau=(np.float32(0.95) / np.maximum(np.float32(1), colsum)).astype(np.float32),
                 sigma=(np.float32(0.95) / np.maximum(np.float32(1), rowsum)).astype(np.float32),
@@ -204,3 +216,21 @@ def plain_iterations(d, iters: int, threads: int = 0) -> None:
         _p(d["ci"], I), _p(d["rv"], F), _p(d["c"], F), _p(d["l"], F), _p(d["u"], F), _p(d["rl"], F),
         _p(d["ru"], F), _p(d["tau"], F), _p(d["sigma"], F), _p(d["x"], F), _p(d["xbar"], F), _p(d["y"], F),
         _p(d["aty"], F), _p(d["axbar"], F), C.c_int(iters), C.c_int(threads))
+
+
+def plain_solve_kkt(d, tol: float, eval_every: int = 100, max_iters: int = 1_000_000, threads: int = 0) -> dict:
+    """The reference algorithm (plain FP32 PDHG, core/src/gpu/cuda_pdhg.cu:14-103
+    with the steps of gpu_solver.cpp:128-151) from its initial point until the
+    FP64 relative KKT of the current (x, y) is <= tol (checked every
+    `eval_every` iterations; the reference's own stopping test off), OpenMP.
+    `d` comes from plain_prepare.  Returns iterations and the KKT triple."""
+    F, I, D = C.c_float, C.c_int, C.c_double
+    out = np.zeros(4)
+    rc = lib().oracle_plain_solve_kkt(
+        C.c_int(d["m"]), C.c_int(d["n"]), _p(d["cp"], I), _p(d["ri"], I), _p(d["cv"], F), _p(d["cv64"], D),
+        _p(d["rp"], I), _p(d["ci"], I), _p(d["rv"], F), _p(d["rv64"], D), _p(d["c64"], D), _p(d["l64"], D),
+        _p(d["u64"], D), _p(d["rl64"], D), _p(d["ru64"], D), C.c_double(tol), C.c_int(eval_every),
+        C.c_int(max_iters), C.c_int(threads), _p(out, D))
+    if rc != 0:
+        raise ValueError("oracle_plain_solve_kkt rejected its arguments")
+    return dict(iterations=int(out[0]), rel_primal=float(out[1]), rel_dual=float(out[2]), rel_gap=float(out[3]))

@@ -61,6 +61,7 @@ typedef struct {
 } oracle_plain_info;
 
 static float maxf_ref(float a, float b) { return (a < b) ? b : a; } /* std::max */
+static int finite_bound_d(double v) { return !isinf(v) && fabs(v) < 1e20; } /* is_bounded_*, problem.hpp:29-35 */
 static float minf_ref(float a, float b) { return (b < a) ? b : a; } /* std::min */
 
 /* cuda_pdhg.cu:14-30 */
@@ -306,6 +307,128 @@ int oracle_plain_iterations(int m, int n, const int* cp, const int* ri, const fl
         csr_spmv(m, rp, ci, rvf, xbar, axbar);
         dual_update(m, sigma, axbar, rl, ru, y);
     }
+    return 0;
+}
+
+/*
+ * The reference algorithm solved to a relative-KKT tolerance (the CPU arm of
+ * the benchmark).  Each iteration is the four kernels of cuda_pdhg.cu:14-103
+ * run as two fused OpenMP passes -- A^T y with the primal update, A x_bar with
+ * the dual update -- with the same float operations in the same order as
+ * oracle_plain_iterations (so the same iterates).  Initial point and step
+ * sizes as oracle_plain_pdhg (gpu_solver.cpp:128-151, entry-order sums).  The
+ * reference's own stopping test is off; every `eval_every` iterations the
+ * FP64 relative KKT of the current (x, y) is computed (the definitions of
+ * oracle_kkt, FP64 matrix values, OpenMP) and the solve stops when all three
+ * terms are <= tol, or after max_iters.  out[0..3] = iterations, rel_p, rel_d,
+ * rel_gap.  Returns 0, or -1 on an invalid argument.
+ */
+static void plain_kkt_f64(int m, int n, const int* cp, const int* ri, const double* cv64, const int* rp,
+                          const int* ci, const double* rv64, const double* c64, const double* l64, const double* u64,
+                          const double* rl64, const double* ru64, double b_inf, double c_inf, const float* x,
+                          const float* y, double* rel) {
+    double rp_inf = 0.0, rd_inf = 0.0, pobj = 0.0, dobj = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : rp_inf, rd_inf) reduction(+ : dobj)
+    for (int i = 0; i < m; ++i) {
+        double a = 0.0, r = 0.0;
+        for (int k = rp[i]; k < rp[i + 1]; ++k) a += rv64[k] * (double)x[ci[k]];
+        if (finite_bound_d(rl64[i]) && a < rl64[i]) r = rl64[i] - a;
+        if (finite_bound_d(ru64[i]) && a > ru64[i]) r = a - ru64[i];
+        rp_inf = fmax(rp_inf, r);
+        const double yi = (double)y[i], yn = yi < 0 ? -yi : 0.0, yp = yi > 0 ? yi : 0.0;
+        if (finite_bound_d(rl64[i])) dobj += yn * rl64[i]; else rd_inf = fmax(rd_inf, yn);
+        if (finite_bound_d(ru64[i])) dobj -= yp * ru64[i]; else rd_inf = fmax(rd_inf, yp);
+    }
+#pragma omp parallel for schedule(static) reduction(max : rd_inf) reduction(+ : dobj, pobj)
+    for (int j = 0; j < n; ++j) {
+        double lam = c64[j];
+        for (int k = cp[j]; k < cp[j + 1]; ++k) lam += cv64[k] * (double)y[ri[k]];
+        pobj += c64[j] * (double)x[j];
+        const double pos = lam > 0 ? lam : 0.0, neg = lam < 0 ? -lam : 0.0;
+        double rd = 0.0;
+        if (finite_bound_d(l64[j])) dobj += pos * l64[j]; else rd = fmax(rd, pos);
+        if (finite_bound_d(u64[j])) dobj -= neg * u64[j]; else rd = fmax(rd, neg);
+        rd_inf = fmax(rd_inf, rd);
+    }
+    rel[0] = rp_inf / (1.0 + b_inf);
+    rel[1] = rd_inf / (1.0 + c_inf);
+    rel[2] = fabs(pobj - dobj) / (1.0 + fabs(pobj) + fabs(dobj));
+}
+
+int oracle_plain_solve_kkt(int m, int n, const int* cp, const int* ri, const float* cvf, const double* cv64,
+                           const int* rp, const int* ci, const float* rvf, const double* rv64, const double* c64,
+                           const double* l64, const double* u64, const double* rl64, const double* ru64, double tol,
+                           int eval_every, int max_iters, int threads, double* out) {
+    if (m <= 0 || n <= 0 || eval_every <= 0 || max_iters < 0 || !out) return -1;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    float *c = malloc(sizeof(float) * n), *l = malloc(sizeof(float) * n), *u = malloc(sizeof(float) * n);
+    float *rl = malloc(sizeof(float) * m), *ru = malloc(sizeof(float) * m);
+    float *tau = malloc(sizeof(float) * n), *sigma = malloc(sizeof(float) * m);
+    float *x = malloc(sizeof(float) * n), *xbar = malloc(sizeof(float) * n), *y = calloc(m, sizeof(float));
+    double b_inf = 0.0, c_inf = 0.0;
+    for (int j = 0; j < n; ++j) {
+        c[j] = (float)c64[j];
+        l[j] = (float)l64[j];
+        u[j] = (float)u64[j];
+        c_inf = fmax(c_inf, fabs(c64[j]));
+        float s = 0.0f;
+        for (int k = cp[j]; k < cp[j + 1]; ++k) s += fabsf(cvf[k]);
+        tau[j] = 0.95f / maxf_ref(1.0f, s);
+        x[j] = maxf_ref(l[j], minf_ref(u[j], 0.0f));
+        xbar[j] = x[j];
+    }
+    for (int i = 0; i < m; ++i) {
+        rl[i] = (float)rl64[i];
+        ru[i] = (float)ru64[i];
+        if (finite_bound_d(rl64[i])) b_inf = fmax(b_inf, fabs(rl64[i]));
+        if (finite_bound_d(ru64[i])) b_inf = fmax(b_inf, fabs(ru64[i]));
+        float s = 0.0f;
+        for (int k = rp[i]; k < rp[i + 1]; ++k) s += fabsf(rvf[k]);
+        sigma[i] = 0.95f / maxf_ref(1.0f, s);
+    }
+    double rel[3] = {INFINITY, INFINITY, INFINITY};
+    int it = 0;
+    while (it < max_iters) {
+        const int stop_at = it + eval_every < max_iters ? it + eval_every : max_iters;
+        for (; it < stop_at; ++it) {
+#pragma omp parallel
+            {
+#pragma omp for schedule(static)
+                for (int j = 0; j < n; ++j) {  /* csc_spmv + primal_update */
+                    float sum = 0.0f;
+                    for (int k = cp[j]; k < cp[j + 1]; ++k) sum += cvf[k] * y[ri[k]];
+                    const float x_old = x[j];
+                    float x_new = x_old - tau[j] * (c[j] + sum);
+                    if (x_new < l[j]) x_new = l[j];
+                    if (x_new > u[j]) x_new = u[j];
+                    x[j] = x_new;
+                    xbar[j] = 2.0f * x_new - x_old;
+                }
+#pragma omp for schedule(static)
+                for (int i = 0; i < m; ++i) {  /* csr_spmv + dual_update */
+                    float sum = 0.0f;
+                    for (int k = rp[i]; k < rp[i + 1]; ++k) sum += rvf[k] * xbar[ci[k]];
+                    const float sig = sigma[i];
+                    const float w = sum + (y[i] / sig);
+                    float p = w;
+                    if (p < rl[i]) p = rl[i];
+                    if (p > ru[i]) p = ru[i];
+                    y[i] = sig * (w - p);
+                }
+            }
+        }
+        plain_kkt_f64(m, n, cp, ri, cv64, rp, ci, rv64, c64, l64, u64, rl64, ru64, b_inf, c_inf, x, y, rel);
+        if (rel[0] <= tol && rel[1] <= tol && rel[2] <= tol) break;
+    }
+    out[0] = (double)it;
+    out[1] = rel[0];
+    out[2] = rel[1];
+    out[3] = rel[2];
+    free(c); free(l); free(u); free(rl); free(ru); free(tau); free(sigma); free(x); free(xbar); free(y);
     return 0;
 }
 

@@ -55,7 +55,13 @@ typedef struct {
 static int fin(double v) { return !isinf(v); }
 static double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+/* OpenMP only on loops whose iterations are independent (SpMV rows / columns,
+ * elementwise updates): the results equal the one-thread run bit for bit; the
+ * reductions stay sequential.  Small LPs run on one thread. */
+#define PAR_MIN 50000
+
 static void mat_x(const mat_t* A, const double* x, double* out) {
+#pragma omp parallel for schedule(static) if (A->m > PAR_MIN)
     for (int i = 0; i < A->m; ++i) {
         double s = 0.0;
         for (int k = A->rp[i]; k < A->rp[i + 1]; ++k) s += A->rv[k] * x[A->ci[k]];
@@ -63,6 +69,7 @@ static void mat_x(const mat_t* A, const double* x, double* out) {
     }
 }
 static void mat_ty(const mat_t* A, const double* y, double* out) {
+#pragma omp parallel for schedule(static) if (A->n > PAR_MIN)
     for (int j = 0; j < A->n; ++j) {
         double s = 0.0;
         for (int k = A->cp[j]; k < A->cp[j + 1]; ++k) s += A->cv[k] * y[A->ri[k]];
@@ -302,6 +309,7 @@ int pdlp_oracle_solve(int64_t m64, int64_t n64, const int64_t* cp64, const int64
         for (int a = 0; a < E; ++a) {
             const double tau = eta / omega, sigma = eta * omega;
             double dx2 = 0, dy2 = 0, inter = 0;
+#pragma omp parallel for schedule(static) if (n > PAR_MIN)
             for (int j = 0; j < n; ++j) xn[j] = clampd(x[j] - tau * (c[j] + kty[j]), l[j], u[j]);
             round_f(xn, n, o->fp32_bits & 1);
             mat_x(&A, xn, kxn);
@@ -336,7 +344,9 @@ int pdlp_oracle_solve(int64_t m64, int64_t n64, const int64_t* cp64, const int64
                 since++;
                 W += eta;
                 const double w = eta / W;
+#pragma omp parallel for schedule(static) if (n > PAR_MIN)
                 for (int j = 0; j < n; ++j) x_avg[j] += w * (x[j] - x_avg[j]);
+#pragma omp parallel for schedule(static) if (m > PAR_MIN)
                 for (int i = 0; i < m; ++i) y_avg[i] += w * (y[i] - y_avg[i]);
                 round_f(x_avg, n, o->fp32_bits & 4);
                 round_f(y_avg, m, o->fp32_bits & 4);

@@ -20,7 +20,16 @@
 # launch syntax by oracle/ref_emul/ref_launchers.cpp.  Nothing else is
 # changed; no reference file is copied into the repository.
 # Usage: oracle/ref_build.sh [reference_dir]   (exits 0 when the reference is absent)
+#        oracle/ref_build.sh --print-dir        prints the reference directory if its
+#                                               sources are there (nothing otherwise)
+# The reference directory is SIH_REFERENCE_DIR, else this recipe's default; the
+# tests and the build entry point ask this recipe for it (oracle.reference_dir()).
 set -euo pipefail
+if [ "${1:-}" = "--print-dir" ]; then
+    R="${SIH_REFERENCE_DIR:-/root/reference}"
+    if [ -d "$R/core/src" ]; then echo "$R"; fi
+    exit 0
+fi
 REF="${1:-${SIH_REFERENCE_DIR:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"

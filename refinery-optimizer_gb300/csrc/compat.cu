@@ -142,54 +142,64 @@ static int split_spmv(int nseg, const int* ptr, const int* idx, const float* val
 
 using namespace sihg;
 
+// Every launcher runs inside guarded(): the lane cache (std::map, std::mutex)
+// and the error messages can throw, and no exception may cross the C ABI.
 extern "C" int sih_pdhg_launch_csr_spmv(int m, const int* d_row_ptr, const int* d_col_ind, const float* d_values,
                                         const float* d_x, float* d_y, void* stream) {
-    return split_spmv(m, d_row_ptr, d_col_ind, d_values, d_x, d_y, stream);
+    return guarded([&] { return split_spmv(m, d_row_ptr, d_col_ind, d_values, d_x, d_y, stream); });
 }
 
 extern "C" int sih_pdhg_launch_csc_spmv(int n, const int* d_col_ptr, const int* d_row_ind, const float* d_values,
                                         const float* d_y, float* d_z, void* stream) {
-    return split_spmv(n, d_col_ptr, d_row_ind, d_values, d_y, d_z, stream);
+    return guarded([&] { return split_spmv(n, d_col_ptr, d_row_ind, d_values, d_y, d_z, stream); });
 }
 
 extern "C" int sih_pdhg_launch_primal_update(int n, const float* d_tau, const float* d_c, const float* d_AT_y,
                                              const float* d_l, const float* d_u, float* d_x, float* d_x_bar,
                                              void* stream) {
-    if (n < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "negative dimension");
-    if (n == 0) return SIH_PDHG_OK;
-    compat_primal_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, d_tau, d_c, d_AT_y, d_l, d_u, d_x,
-                                                                             d_x_bar);
-    SIHG_LAUNCH_CHECK();
-    return SIH_PDHG_OK;
+    return guarded([&]() -> int {
+        if (n < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "negative dimension");
+        if (n == 0) return SIH_PDHG_OK;
+        compat_primal_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, d_tau, d_c, d_AT_y, d_l, d_u, d_x,
+                                                                                 d_x_bar);
+        SIHG_LAUNCH_CHECK();
+        return SIH_PDHG_OK;
+    });
 }
 
 extern "C" int sih_pdhg_launch_dual_update(int m, const float* d_sigma, const float* d_A_xbar, const float* d_row_l,
                                            const float* d_row_u, float* d_y, void* stream) {
-    if (m < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "negative dimension");
-    if (m == 0) return SIH_PDHG_OK;
-    compat_dual_kernel<<<grid_for(m, 256), 256, 0, (cudaStream_t)stream>>>(m, d_sigma, d_A_xbar, d_row_l, d_row_u,
-                                                                           d_y);
-    SIHG_LAUNCH_CHECK();
-    return SIH_PDHG_OK;
+    return guarded([&]() -> int {
+        if (m < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "negative dimension");
+        if (m == 0) return SIH_PDHG_OK;
+        compat_dual_kernel<<<grid_for(m, 256), 256, 0, (cudaStream_t)stream>>>(m, d_sigma, d_A_xbar, d_row_l, d_row_u,
+                                                                               d_y);
+        SIHG_LAUNCH_CHECK();
+        return SIH_PDHG_OK;
+    });
 }
 
 extern "C" int sih_pdhg_launch_restart(int n, const float* d_x, float* d_x_bar, void* stream) {
-    if (n < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "negative dimension");
-    if (n == 0) return SIH_PDHG_OK;
-    compat_copy_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, d_x, d_x_bar);
-    SIHG_LAUNCH_CHECK();
-    return SIH_PDHG_OK;
+    return guarded([&]() -> int {
+        if (n < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "negative dimension");
+        if (n == 0) return SIH_PDHG_OK;
+        compat_copy_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(n, d_x, d_x_bar);
+        SIHG_LAUNCH_CHECK();
+        return SIH_PDHG_OK;
+    });
 }
 
 extern "C" int sih_pdhg_launch_residuals(int m, int n, const float* d_Ax, const float* d_row_l, const float* d_row_u,
                                          float* d_row_viols, const float* d_x, const float* d_c, const float* d_AT_y,
                                          const float* d_l, const float* d_u, const float* d_tau, float* d_col_viols,
                                          void* stream) {
-    if (m < 0 || n < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "negative dimension");
-    cudaStream_t s = (cudaStream_t)stream;
-    if (m > 0) compat_row_viol_kernel<<<grid_for(m, 256), 256, 0, s>>>(m, d_Ax, d_row_l, d_row_u, d_row_viols);
-    if (n > 0)
-        compat_col_viol_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, d_x, d_c, d_AT_y, d_l, d_u, d_tau, d_col_viols);
-    SIHG_LAUNCH_CHECK();
-    return SIH_PDHG_OK;
+    return guarded([&]() -> int {
+        if (m < 0 || n < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "negative dimension");
+        cudaStream_t s = (cudaStream_t)stream;
+        if (m > 0) compat_row_viol_kernel<<<grid_for(m, 256), 256, 0, s>>>(m, d_Ax, d_row_l, d_row_u, d_row_viols);
+        if (n > 0)
+            compat_col_viol_kernel<<<grid_for(n, 256), 256, 0, s>>>(n, d_x, d_c, d_AT_y, d_l, d_u, d_tau, d_col_viols);
+        SIHG_LAUNCH_CHECK();
+        return SIH_PDHG_OK;
+    });
 }

@@ -60,40 +60,78 @@ static int grid_for(int n, int per_block, int sms) {
     return std::max(1, std::min((n + per_block - 1) / per_block, sms * 8));
 }
 
-// Device address of g_check_scratch, looked up once per device with that
-// device current (host code must not use the symbol itself as an address).
-static int scratch_address(float** out, int* sms) {
-    constexpr int kMaxDevices = 64;
-    static std::mutex mu;
-    static float* addr[kMaxDevices] = {};
-    static int sm_count[kMaxDevices] = {};
-    int dev = 0;
-    SIHG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return fail(SIH_PDHG_ERR_UNSUPPORTED, "device ordinal beyond 63");
-    std::lock_guard<std::mutex> g(mu);
-    if (!addr[dev]) {
-        void* p = nullptr;
-        SIHG_CUDA(cudaGetSymbolAddress(&p, g_check_scratch));
-        int s = 0;
-        SIHG_CUDA(cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev));
-        addr[dev] = static_cast<float*>(p);
-        sm_count[dev] = s;
-    }
-    *out = addr[dev];
-    *sms = sm_count[dev];
+// Id of the calling thread's current CUDA context (cuCtxGetId: unique for the
+// life of the process, so a context re-created after cudaDeviceReset gets a
+// new one).  The two driver calls are looked up through the runtime, so the
+// library does not link the driver library itself.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+static int current_context_id(unsigned long long* id) {
+    static std::once_flag once;
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    if (!get_current || !get_id) return fail(SIH_PDHG_ERR_CUDA, "driver entry points cuCtxGetCurrent / cuCtxGetId unavailable");
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0) return fail(SIH_PDHG_ERR_CUDA, "cuCtxGetCurrent failed");
+    *id = 0;  // no context current yet: the runtime creates it at the first call that needs one
+    if (ctx && get_id(ctx, id) != 0) return fail(SIH_PDHG_ERR_CUDA, "cuCtxGetId failed");
     return SIH_PDHG_OK;
 }
 
-}  // namespace sihg
+// Device address of g_check_scratch (host code must not use the symbol itself
+// as an address).  Set-up, with the device current: once per device, and again
+// when the device's context is a new one (after cudaDeviceReset the module is
+// loaded again and the array may sit elsewhere).  Later calls only compare the
+// context id.
+static int scratch_address(float** out, int* sms) {
+    constexpr int kMaxDevices = 64;
+    struct Entry {
+        unsigned long long ctx_id = 0;
+        float* addr = nullptr;
+        int sm_count = 0;
+    };
+    static std::mutex mu;
+    static Entry table[kMaxDevices];
+    int dev = 0;
+    SIHG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(SIH_PDHG_ERR_UNSUPPORTED, "device ordinal beyond 63");
+    unsigned long long ctx_id = 0;
+    SIHG_TRY(current_context_id(&ctx_id));
+    std::lock_guard<std::mutex> g(mu);
+    Entry& e = table[dev];
+    if (!e.addr || ctx_id == 0 || e.ctx_id != ctx_id) {
+        void* p = nullptr;
+        SIHG_CUDA(cudaGetSymbolAddress(&p, g_check_scratch));  // makes the primary context current if none was
+        if (ctx_id == 0) SIHG_TRY(current_context_id(&ctx_id));
+        int s = 0;
+        SIHG_CUDA(cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev));
+        e.addr = static_cast<float*>(p);
+        e.sm_count = s;
+        e.ctx_id = ctx_id;
+    }
+    *out = e.addr;
+    *sms = e.sm_count;
+    return SIH_PDHG_OK;
+}
 
-using namespace sihg;
-
-extern "C" int sih_pdhg_check_norms_noalloc(int m, int n, int nnz, const int* d_row_ptr, const int* d_col_ind,
-                                            const float* d_csr_values, const int* d_col_ptr, const int* d_row_ind,
-                                            const float* d_csc_values, const float* d_x, const float* d_y,
-                                            const float* d_c, const float* d_l, const float* d_u,
-                                            const float* d_tau, const float* d_row_l, const float* d_row_u,
-                                            float max_abs_b, float max_abs_c, float* d_out, void* stream) {
+static int check_norms_noalloc_impl(int m, int n, int nnz, const int* d_row_ptr, const int* d_col_ind,
+                                    const float* d_csr_values, const int* d_col_ptr, const int* d_row_ind,
+                                    const float* d_csc_values, const float* d_x, const float* d_y, const float* d_c,
+                                    const float* d_l, const float* d_u, const float* d_tau, const float* d_row_l,
+                                    const float* d_row_u, float max_abs_b, float max_abs_c, float* d_out,
+                                    void* stream) {
     if (m < 1 || n < 1 || nnz < 0) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "m and n must be >= 1, nnz >= 0");
     if ((long long)m + (long long)n > kNoAllocMaxRowsCols)
         return fail(SIH_PDHG_ERR_INVALID_ARGUMENT,
@@ -124,4 +162,21 @@ extern "C" int sih_pdhg_check_norms_noalloc(int m, int n, int nnz, const int* d_
     noalloc_finish_kernel<<<1, 32, 0, s>>>(words, max_abs_b, max_abs_c, d_out);
     SIHG_LAUNCH_CHECK();
     return SIH_PDHG_OK;
+}
+
+}  // namespace sihg
+
+using namespace sihg;
+
+extern "C" int sih_pdhg_check_norms_noalloc(int m, int n, int nnz, const int* d_row_ptr, const int* d_col_ind,
+                                            const float* d_csr_values, const int* d_col_ptr, const int* d_row_ind,
+                                            const float* d_csc_values, const float* d_x, const float* d_y,
+                                            const float* d_c, const float* d_l, const float* d_u,
+                                            const float* d_tau, const float* d_row_l, const float* d_row_u,
+                                            float max_abs_b, float max_abs_c, float* d_out, void* stream) {
+    return guarded([&] {
+        return check_norms_noalloc_impl(m, n, nnz, d_row_ptr, d_col_ind, d_csr_values, d_col_ptr, d_row_ind,
+                                        d_csc_values, d_x, d_y, d_c, d_l, d_u, d_tau, d_row_l, d_row_u, max_abs_b,
+                                        max_abs_c, d_out, stream);
+    });
 }

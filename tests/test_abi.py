@@ -192,6 +192,12 @@ int main(int argc, char** argv) {
     r.row_duals = y;
     int rc = sih_pdhg_solve_ex(&p, &cfg, &opt, &r);
     printf("solve %d %d %.9g\n", rc, r.status, r.primal_objective);
+    sih_pdhg_result rp = {0};
+    rp.x = x;
+    rp.row_duals = y;
+    rc = sih_pdhg_solve(&p, &cfg, &rp); /* the GpuSolver::solve_pdhg drop-in (reference algorithm) */
+    printf("plain %d %d %.9g %lld %.9g %.9g\n", rc, rp.status, rp.primal_objective, (long long)rp.iterations,
+           x[0], x[1]);
     free(x);
     free(y);
     sih_pdhg_mps_free(mps);
@@ -200,12 +206,9 @@ int main(int argc, char** argv) {
 """
 
 
-def test_plain_c_client_reads_mps_and_calls_the_solver(tmp_path):
-    """The ABI from C (no C++ or Python in between): read an MPS file into a
-    sih_pdhg_problem view and hand it to sih_pdhg_solve_ex.  Without a device
-    the solve returns SIH_PDHG_ERR_NO_DEVICE after the problem was accepted;
-    with one it solves (min -x1 - 2 x2, x1 + x2 <= 4, x1 - x2 <= -1, x >= 0:
-    optimum -8 at (0, 4))."""
+def _run_c_client(tmp_path):
+    """Compiles the C client against the library and runs it on a toy MPS file:
+    min -x1 - 2 x2, x1 + x2 <= 4, x1 - x2 <= -1, x >= 0 (optimum -8 at (0, 4))."""
     from sih_pdhg import _lib
 
     lib_path = _lib.LIB_PATH
@@ -222,8 +225,33 @@ def test_plain_c_client_reads_mps_and_calls_the_solver(tmp_path):
     assert out.returncode == 0, out.stdout + out.stderr
     lines = dict(l.split(" ", 1) for l in out.stdout.splitlines())
     assert lines["problem"] == "toy 2 2 4 0 1 0"
+    return lines
+
+
+def test_plain_c_client_reads_mps_and_calls_the_solver(tmp_path):
+    """The ABI from C (no C++ or Python in between): read an MPS file into a
+    sih_pdhg_problem view and hand it to sih_pdhg_solve_ex and sih_pdhg_solve.
+    Without a device both return SIH_PDHG_ERR_NO_DEVICE after the problem was
+    accepted (no CPU fallback)."""
+    from sih_pdhg import _lib
+
+    lib = _lib.load()
+    if lib.sih_pdhg_is_cuda_available():
+        pytest.skip("device present: the GPU-marked test below runs the solves")
+    lines = _run_c_client(tmp_path)
+    assert lines["solve"].split()[0] == "2"
+    assert lines["plain"].split()[0] == "2"
+
+
+@pytest.mark.gpu
+def test_plain_c_client_solves_on_the_gpu(tmp_path):
+    """Same C client on a GPU: the mixed solve and the drop-in for
+    GpuSolver::solve_pdhg (reference algorithm and config defaults) both reach
+    the optimum -8 at (0, 4)."""
+    lines = _run_c_client(tmp_path)
     rc, status, obj = lines["solve"].split()
-    if int(rc) == 2:  # SIH_PDHG_ERR_NO_DEVICE: validation passed, no CPU fallback
-        return
-    assert int(rc) == 0 and int(status) == 0
+    assert int(rc) == 0 and int(status) == 0, lines["solve"]
     assert abs(float(obj) - (-8.0)) <= 1e-3
+    rc, status, obj, iters, x0, x1 = lines["plain"].split()
+    assert int(rc) == 0 and int(status) == 0, lines["plain"]
+    assert abs(float(obj) - (-8.0)) <= 1e-3 and abs(float(x0)) <= 1e-3 and abs(float(x1) - 4.0) <= 1e-3

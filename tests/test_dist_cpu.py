@@ -63,12 +63,19 @@ def test_reference_arm_under_torchrun_world_size_2():
     assert d["e2e"]["h2d_bytes_per_step"] == 0
 
 
-def test_reference_arm_on_an_mps_workload_reports_unavailable():
-    """`--workload mps:PATH` reads an MPS file; the reference arm has no measured
-    iteration count for it and says so in its one JSON line (exit 0)."""
-    path = os.path.join(REPO, "tests", "golden", "mps", "edge_values.mps")
+def test_reference_arm_solves_an_mps_workload_to_tolerance(tmp_path):
+    """`--workload mps:PATH` reads an MPS file; the reference arm solves it with
+    the plain algorithm's CPU port until the relative KKT reaches the tolerance
+    (or the iteration cap, flagged as a lower bound) and prints one JSON line."""
+    path = tmp_path / "toy.mps"  # min -x1 - 2 x2, x1 + x2 <= 4, x1 - x2 <= -1, x >= 0
+    path.write_text("NAME toy\nROWS\n N  OBJ\n L  R1\n L  R2\nCOLUMNS\n    X1  OBJ  -1.0  R1  1.0\n"
+                    "    X1  R2  1.0\n    X2  OBJ  -2.0  R1  1.0\n    X2  R2  -1.0\nRHS\n    RHS  R1  4.0  R2  -1.0\n"
+                    "ENDATA\n")
     r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--workload",
-                        f"mps:{path}"], capture_output=True, text=True, timeout=300, cwd=REPO)
+                        f"mps:{path}", "--steps", "2", "--warmup", "1"], capture_output=True, text=True, timeout=300,
+                       cwd=REPO)
     assert r.returncode == 0, r.stderr[-2000:]
     d = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][0])
-    assert d["impl"] == "reference" and "unavailable" in d
+    assert d["impl"] == "reference" and d["value"] > 0 and d["iterations"] > 0
+    assert d["config"]["workload"].startswith("mps:")
+    assert d["reached_tol"] and max(d["rel_kkt"]) <= d["config"]["tol"]

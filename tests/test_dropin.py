@@ -9,9 +9,10 @@ import sys
 
 import pytest
 
+import oracle  # test infrastructure: locates the reference sources
 from conftest import REPO
 
-REF = os.environ.get("SIH_REFERENCE_DIR", "/root/reference")
+REF = oracle.reference_dir() or ""  # the reference sources, where present (this build's recipe knows where)
 ENGINE_CORE = os.path.join(REPO, "oracle", "_ref", "engine")
 
 

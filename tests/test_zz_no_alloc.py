@@ -29,7 +29,7 @@ def env():
     return torch, _lib.load(), sih_pdhg
 
 
-def _device_problem(torch, seed, m, n, k):
+def _device_problem(torch, seed, m, n, k, nan_cost_column=None):
     from sih_pdhg.generators import small_random_lp
 
     p = small_random_lp(m, n, k, seed)
@@ -42,10 +42,12 @@ def _device_problem(torch, seed, m, n, k):
                 c=p.c.astype(np.float32), l=p.col_lower.astype(np.float32), u=p.col_upper.astype(np.float32),
                 tau=rng.uniform(0.01, 0.5, n).astype(np.float32), rl=p.row_lower.astype(np.float32),
                 ru=p.row_upper.astype(np.float32))
+    if nan_cost_column is not None:  # that column's measure is NaN; the row side is untouched
+        host["c"][nan_cost_column] = np.nan
     dev = {k2: torch.from_numpy(v).cuda() for k2, v in host.items()}
     max_b = np.float32(max(1.0, np.abs(np.concatenate([host["ru"][host["ru"] < 1e15],
                                                         host["rl"][host["rl"] > -1e15]])).max()))
-    max_c = np.float32(max(1.0, np.abs(host["c"]).max()))
+    max_c = np.float32(max(1.0, np.nanmax(np.abs(host["c"]))))
     return p, dev, max_b, max_c
 
 
@@ -68,8 +70,9 @@ def _allocating_route(torch, lib, p, d, max_b, max_c):
     return np.float32(max_p / max_b), np.float32(max_d / max_c)
 
 
-def _no_alloc_route(torch, lib, p, d, max_b, max_c):
-    out = torch.full((2,), -1.0, dtype=torch.float32, device="cuda")
+def _no_alloc_route(torch, lib, p, d, max_b, max_c, out=None):
+    if out is None:
+        out = torch.full((2,), -1.0, dtype=torch.float32, device="cuda")
     rc = lib.sih_pdhg_check_norms_noalloc(
         p.num_rows(), p.num_cols(), p.num_nonzeros(), d["rp"].data_ptr(), d["ci"].data_ptr(), d["rv"].data_ptr(),
         d["cp"].data_ptr(), d["ri"].data_ptr(), d["cv"].data_ptr(), d["x"].data_ptr(), d["y"].data_ptr(),
@@ -98,3 +101,33 @@ def test_no_alloc_rejects_sizes_beyond_its_limit(env):
                                           None, None)
     assert rc == 1
     assert b"no-alloc limit" in lib.sih_pdhg_last_error()
+
+
+def test_no_alloc_skips_a_nan_column_measure(env):
+    """A NaN in one column's cost makes that column's measure NaN; the reference's
+    host loop (gpu_solver.cpp:249-259) keeps its running maximum on a NaN, and so
+    does the no-alloc check: both routes give the same finite maxima."""
+    torch, lib, _ = env
+    p, d, max_b, max_c = _device_problem(torch, 21, 500, 1200, 8, nan_cost_column=37)
+    ref = _allocating_route(torch, lib, p, d, max_b, max_c)
+    got = _no_alloc_route(torch, lib, p, d, max_b, max_c)
+    assert np.all(np.isfinite(got)) and got[1] > 0
+    np.testing.assert_allclose(got, np.array(ref, dtype=np.float32), rtol=1e-6, atol=0)
+
+
+def test_no_alloc_calls_leave_device_memory_unchanged(env):
+    """After the first call on the device (which may make CUDA load the library's
+    device code and place the array), further calls allocate nothing: the
+    device's free memory reads the same before and after them."""
+    torch, lib, _ = env
+    p, d, max_b, max_c = _device_problem(torch, 31, 800, 2000, 8)
+    out = torch.full((2,), -1.0, dtype=torch.float32, device="cuda")
+    first = _no_alloc_route(torch, lib, p, d, max_b, max_c, out)
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        got = _no_alloc_route(torch, lib, p, d, max_b, max_c, out)
+        np.testing.assert_array_equal(got, first)
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, (free_before, free_after)
