@@ -135,7 +135,10 @@ typedef struct sih_pdhg_options {
                                   a gathered vector, so that gathers of the longest segments of the other side
                                   skip L2; the step SpMVs then run one 1024-thread block per SM.  0 = automatic
                                   (on where the staged entries carry a large share of the nonzeros), -1 = off */
-    int32_t reserved1;         /* 0 */
+    int32_t persistent;        /* mixed: 1 = run the steps between two evaluations as ONE persistent cooperative
+                                  kernel (phases separated by grid barriers with bounded waits; for LPs and batch
+                                  tails whose steps are latency-bound); 0 = one kernel per phase, replayed as CUDA
+                                  graphs (default).  Same iterates either way. */
 } sih_pdhg_options;
 
 /*
@@ -238,6 +241,16 @@ int sih_pdhg_set_start(sih_pdhg_handle* h, int32_t index, const double* x, const
  * options.autotune = 1). */
 int sih_pdhg_get_task_nnz(const sih_pdhg_handle* h, int32_t* task_nnz);
 void sih_pdhg_destroy(sih_pdhg_handle* h);
+
+/* Self-test of the grid barrier of the persistent step kernel
+ * (options.persistent; no counterpart in the reference, whose iteration loop
+ * has no device-side waits): `rounds` barriers on a cooperative grid of
+ * `blocks` blocks that waits for `blocks + missing` arrivals, every wait
+ * bounded by limit_sec (at most 10 s).  With missing > 0 no barrier can
+ * complete: each block's wait runs out, the kernel returns, *timed_out gets 1
+ * and the device stays usable.  *passed gets the barriers completed. */
+int sih_pdhg_check_grid_barrier(int32_t blocks, int32_t missing, int32_t rounds, double limit_sec,
+                                int32_t* timed_out, int32_t* passed);
 
 /* One-call batch: create + run + result for each instance + destroy.
  * results[count] (arrays inside each may be NULL). */

@@ -152,6 +152,18 @@ int sih_pdhg_get_task_nnz(const sih_pdhg_handle* h, int32_t* task_nnz) {
 
 void sih_pdhg_destroy(sih_pdhg_handle* h) { delete h; }
 
+int sih_pdhg_check_grid_barrier(int32_t blocks, int32_t missing, int32_t rounds, double limit_sec,
+                                int32_t* timed_out, int32_t* passed) {
+    return guarded([&]() -> int {
+        if (!device_present()) return fail(SIH_PDHG_ERR_NO_DEVICE, "no CUDA device");
+        int t = 0, p = 0;
+        SIHG_TRY(check_grid_barrier(blocks, missing, rounds, limit_sec, &t, &p));
+        if (timed_out) *timed_out = t;
+        if (passed) *passed = p;
+        return SIH_PDHG_OK;
+    });
+}
+
 static int solve_batch_impl(const sih_pdhg_problem* problems, int32_t count, const sih_pdhg_config* config,
                          const sih_pdhg_options* opts, sih_pdhg_result* results) {
     if (!results) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "results is NULL");

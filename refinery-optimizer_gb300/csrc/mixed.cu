@@ -38,6 +38,7 @@
 #include <tuple>
 
 #include "mixed.h"
+#include "gridsync.cuh"
 #include "warp.cuh"
 
 namespace sihg {
@@ -91,13 +92,12 @@ __device__ __forceinline__ StepScalars step_scalars(const Inst& S) {
     return StepScalars{S.cur, S.avg_pending, S.restart_flag, (float)S.avg_w, (float)(S.eta / S.omega)};
 }
 
-__global__ void __launch_bounds__(kThreads) k_step_primal(int B, Chunks ch, Vecs V, Inst* __restrict__ st) {
-    chain_wait();
-    // chunks as for_each_element; every thread loads the operands of U = 4
+template <int U>
+__device__ __forceinline__ void step_primal_body(const Chunks& ch, const Vecs& V, const Inst* st) {
+    // chunks as for_each_element; every thread loads the operands of U
     // elements of its chunk before it stores any of them (the stores would
     // otherwise keep the next element's loads behind them: one DRAM latency
     // per element)
-    constexpr int U = 4;
     __shared__ StepScalars sh;
     const int nact = *ch.nactive;
     for (int c = blockIdx.x; c < nact; c += gridDim.x) {
@@ -160,6 +160,11 @@ __global__ void __launch_bounds__(kThreads) k_step_primal(int B, Chunks ch, Vecs
             }
         }
     }
+}
+
+__global__ void __launch_bounds__(kThreads) k_step_primal(int B, Chunks ch, Vecs V, Inst* __restrict__ st) {
+    chain_wait();
+    step_primal_body<4>(ch, V, st);
 }
 
 // The step-size schedule factors k^-0.6 and k^-0.3 of this attempt (k =
@@ -319,6 +324,52 @@ __global__ void __launch_bounds__(kStagedThreads, 1)
     stage_prefix(pick(V.y0, V.y1, st[0].cur ^ 1), staged);
     KtyStepEpiStaged epi{{V}, staged};
     spmv_engine<1, true, 2>(cols, st, epi, 0u);
+}
+
+// Persistent form of the step loop (options.persistent): one cooperative
+// launch runs `nsteps` steps, each as the three phases of the kernels above
+// (elementwise primal step, K x' with the dual step, K^T y' with the step-size
+// controller) separated by grid barriers instead of kernel boundaries.  The
+// gathered vectors are written inside the launch, so the epilogues gather
+// through the coherent path.  Same tasks, same reduction order and same
+// controller as the separate kernels, so the iterates are bit-identical.
+struct DualStepEpiCoherent : DualStepEpi {
+    static constexpr bool kCoherent = true;
+};
+struct KtyStepEpiCoherent : KtyStepEpi {
+    static constexpr bool kCoherent = true;
+};
+
+__global__ void __launch_bounds__(kThreads, 4)
+    k_steps_persistent(int B, int nsteps, Chunks ch, Side rows, Side cols, Vecs V, Inst* st, GridBar gb) {
+    if (ld_status(gb.status) != 0) return;  // an earlier launch of this run timed out
+    unsigned gen = grid_gen(gb);
+    for (int k = 0; k < nsteps; ++k) {
+        step_primal_body<2>(ch, V, st);
+        if (!grid_barrier(gb, gen)) return;
+        step_schedule_pows(B, st);
+        {
+            DualStepEpiCoherent epi{{V}};
+            spmv_engine<1, true, 1>(rows, st, epi, 0u);
+        }
+        if (!grid_barrier(gb, gen)) return;
+        {
+            KtyStepEpiCoherent epi{{V}};
+            spmv_engine<1, true, 2>(cols, st, epi, 0u);
+        }
+        if (k + 1 < nsteps && !grid_barrier(gb, gen)) return;
+    }
+}
+
+// Barrier self-test (sih_pdhg_check_grid_barrier): `rounds` grid barriers;
+// with gb.expected above the grid no barrier completes and every block's
+// bounded wait runs out.
+__global__ void k_barrier_probe(GridBar gb, int rounds, unsigned* passed) {
+    unsigned gen = grid_gen(gb);
+    for (int r = 0; r < rounds; ++r) {
+        if (!grid_barrier(gb, gen)) return;
+        if (threadIdx.x == 0) atomicAdd(passed, 1u);
+    }
 }
 
 // ---------------------------------------------------------------- evaluation kernels
@@ -1267,6 +1318,84 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     }
     phase("state");
     if (opts.autotune && opts.tile_nnz <= 0) SIHG_TRY(autotune());
+    SIHG_TRY(setup_persistent());
+    return SIH_PDHG_OK;
+}
+
+// Persistent step kernel: every block must be resident at once (a
+// cooperative launch checks it), so the grid is the SM count times the
+// kernel's occupancy; the barrier words are reset at the start of each run.
+int MixedSolver::setup_persistent() {
+    persistent_ = 0;
+    if (opts_.persistent == 0) return SIH_PDHG_OK;
+    int dev = 0, coop = 0, occ = 0;
+    SIHG_CUDA(cudaGetDevice(&dev));
+    SIHG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return fail(SIH_PDHG_ERR_UNSUPPORTED, "options.persistent: the device has no cooperative launch");
+    SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_steps_persistent, kThreads, 0));
+    if (occ < 1) return fail(SIH_PDHG_ERR_UNSUPPORTED, "options.persistent: the step kernel does not fit on an SM");
+    pgrid_ = sm_count_ * occ;
+    SIHG_TRY(bar_.alloc(4 * sizeof(unsigned)));
+    persistent_ = 1;
+    return SIH_PDHG_OK;
+}
+
+// Longest wait of one grid barrier of the persistent kernel.  A phase of the
+// largest batch this engine holds takes milliseconds; a wait this long means
+// a block stopped arriving.
+constexpr double kBarrierLimitSec = 2.0;
+
+static GridBar make_bar(const DevMem& words, unsigned expected, double limit_sec) {
+    unsigned* w = words.as<unsigned>();
+    return GridBar{w, w + 1, reinterpret_cast<int*>(w + 2), expected,
+                   (unsigned long long)(limit_sec * 1e9)};
+}
+
+// One cooperative launch of the persistent step kernel: `nsteps` steps.
+int MixedSolver::launch_persistent(cudaStream_t s, int nsteps) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)pgrid_);
+    cfg.blockDim = dim3((unsigned)kThreads);
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const GridBar gb = make_bar(bar_, (unsigned)pgrid_, kBarrierLimitSec);
+    SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_steps_persistent, B_, nsteps, chunks_all_, rows_, cols_, V_,
+                                 state_.as<Inst>(), gb));
+    launches_ += 1;
+    return SIH_PDHG_OK;
+}
+
+int check_grid_barrier(int blocks, int missing, int rounds, double limit_sec, int* timed_out, int* passed) {
+    if (blocks < 1 || missing < 0 || rounds < 1 || !(limit_sec > 0.0) || limit_sec > 10.0)
+        return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "grid barrier check: blocks >= 1, missing >= 0, rounds >= 1, "
+                                                   "0 < limit_sec <= 10");
+    int dev = 0, sms = 0, occ = 0;
+    SIHG_CUDA(cudaGetDevice(&dev));
+    SIHG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_barrier_probe, kThreads, 0));
+    if (blocks > sms * occ) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "grid barrier check: more blocks than fit");
+    DevMem words;
+    SIHG_TRY(words.alloc(8 * sizeof(unsigned)));
+    SIHG_CUDA(cudaMemset(words.as<void>(), 0, 8 * sizeof(unsigned)));
+    const GridBar gb = make_bar(words, (unsigned)(blocks + missing), limit_sec);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3((unsigned)kThreads);
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_barrier_probe, gb, rounds, words.as<unsigned>() + 4));
+    SIHG_CUDA(cudaDeviceSynchronize());
+    unsigned h[8];
+    SIHG_CUDA(cudaMemcpy(h, words.as<void>(), sizeof(h), cudaMemcpyDeviceToHost));
+    if (timed_out) *timed_out = (int)h[2];
+    if (passed) *passed = (int)(h[4] / (unsigned)blocks);
     return SIH_PDHG_OK;
 }
 
@@ -1456,7 +1585,9 @@ int MixedSolver::record_graph() {
 
 int MixedSolver::run() {
     eval_freq_ = opts_.eval_frequency > 0 ? opts_.eval_frequency : 64;
-    if (opts_.use_graph) SIHG_TRY(record_graph());
+    const bool graph = opts_.use_graph && !persistent_;
+    if (graph) SIHG_TRY(record_graph());
+    if (persistent_) SIHG_CUDA(cudaMemsetAsync(bar_.as<void>(), 0, 4 * sizeof(unsigned), stream_));
     const auto t0 = std::chrono::steady_clock::now();
     launches_ = 0;
     SIHG_TRY(reset_state());
@@ -1489,7 +1620,10 @@ int MixedSolver::run() {
                     break;
                 }
             }
-            if (opts_.use_graph) {
+            if (persistent_) {
+                rc = launch_persistent(s, eval_freq_);
+                if (rc == SIH_PDHG_OK) rc = launch_eval(s);
+            } else if (graph) {
                 cudaError_t e = cudaGraphLaunch(graphs_[0], s);
                 if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
                 launches_ += 3ull * eval_freq_ + 6ull;
@@ -1508,6 +1642,13 @@ int MixedSolver::run() {
         if (ev[w]) cudaEventDestroy(ev[w]);
     cudaFreeHost(h_done);
     if (rc != SIH_PDHG_OK) return rc;
+    if (persistent_) {
+        int status = 0;
+        SIHG_CUDA(cudaMemcpy(&status, bar_.as<unsigned>() + 2, sizeof(int), cudaMemcpyDeviceToHost));
+        if (status != 0)
+            return fail(SIH_PDHG_ERR_CUDA, "persistent step kernel: a grid barrier wait ran out (a block stopped "
+                                           "arriving); the solve was abandoned");
+    }
     SIHG_CUDA(cudaMemcpy(host_inst_.data(), state_.as<Inst>(), sizeof(Inst) * B_, cudaMemcpyDeviceToHost));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev_start_, ev_stop_);

@@ -162,6 +162,7 @@ class MixedSolver {
     int time_kernels(int reps, double* seconds, double* bytes);
     int set_start(int b, const double* x, const double* y, double omega);
     int task_nnz() const { return task_nnz_; }
+    bool persistent() const { return persistent_ != 0; }
     long long nnz() const { return nnz_; }
     int rows() const { return M_; }
     int cols() const { return N_; }
@@ -174,6 +175,8 @@ class MixedSolver {
     int record_graph();
     int choose_staging();
     int launch_step_spmvs(cudaStream_t s, int which);
+    int launch_persistent(cudaStream_t s, int nsteps);
+    int setup_persistent();
 
     std::vector<const HostProblem*> probs_;
     sih_pdhg_config cfg_{};
@@ -202,10 +205,20 @@ class MixedSolver {
     // staged gathers (single LP): entries of x (for K x) and of y (for K^T y)
     // copied to shared memory by every block of the step kernels; 0 = off
     int stage_x_ = 0, stage_y_ = 0;
+    // persistent step kernel (options.persistent): its grid (every block
+    // resident) and the grid barrier's words {arrive, gen, status}
+    int persistent_ = 0, pgrid_ = 0;
+    DevMem bar_;
     Vecs V_{};
     std::vector<Inst> host_inst_;
     std::vector<std::vector<float>> start_x_, start_y_;  // warm starts (device order, unscaled)
 };
+
+// Runs `rounds` grid barriers of the persistent kernel on a cooperative grid
+// of `blocks` blocks that waits for `blocks + missing` arrivals, each wait
+// bounded by limit_sec: with missing > 0 every wait runs out.  *timed_out gets
+// the barrier's status word, *passed the barriers block 0 passed.
+int check_grid_barrier(int blocks, int missing, int rounds, double limit_sec, int* timed_out, int* passed);
 
 int solve_mixed(const HostProblem& hp, const sih_pdhg_config& cfg, const sih_pdhg_options& opts,
                 sih_pdhg_result* r);

@@ -71,9 +71,27 @@ struct Staged<Epi, decltype(void(Epi::kStaged))> {
     static constexpr bool value = Epi::kStaged;
 };
 
+// Coherent gathers.  An epilogue with `kCoherent = true` runs inside the
+// persistent step kernel, where the gathered vector was written earlier in the
+// same launch (before a grid barrier): its gathers use ordinary global loads,
+// which the barrier's fences order, instead of the read-only (.nc) path that
+// is only valid for data no thread of the launch writes.
+template <class Epi, class = void>
+struct Coherent {
+    static constexpr bool value = false;
+};
+template <class Epi>
+struct Coherent<Epi, decltype(void(Epi::kCoherent))> {
+    static constexpr bool value = Epi::kCoherent;
+};
+
 template <class Epi>
 __device__ __forceinline__ float gather_one(const Epi& epi, const float* __restrict__ vec, int idx) {
-    if constexpr (Staged<Epi>::value) {
+    if constexpr (Coherent<Epi>::value) {
+        float v;
+        asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(vec + idx));
+        return v;
+    } else if constexpr (Staged<Epi>::value) {
         // predicated loads, no branch: the shared copy below `staged`, else
         // the vector (the gathers of a batch then issue back to back)
         extern __shared__ float stage_vec[];

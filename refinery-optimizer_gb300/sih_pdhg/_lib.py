@@ -48,7 +48,7 @@ class COptions(C.Structure):
                 ("primal_weight_smoothing", C.c_double), ("exact_arithmetic", C.c_int32),
                 ("lanes_csr", C.c_int32), ("lanes_csc", C.c_int32), ("heavy_factor", C.c_int32),
                 ("tile_nnz", C.c_int32), ("reorder", C.c_int32), ("staged_kib", C.c_int32),
-                ("reserved1", C.c_int32)]
+                ("persistent", C.c_int32)]
 
 
 class CAdjointOptions(C.Structure):
@@ -116,6 +116,8 @@ def load() -> C.CDLL:
     lib.sih_pdhg_time_kernels.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.sih_pdhg_set_start.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double]
     lib.sih_pdhg_get_task_nnz.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    lib.sih_pdhg_check_grid_barrier.argtypes = [i32, i32, i32, C.c_double, C.POINTER(C.c_int32),
+                                                C.POINTER(C.c_int32)]
     lib.sih_pdhg_adjoint_options_default.argtypes = [C.c_void_p]
     lib.sih_pdhg_adjoint_options_default.restype = None
     pp = C.POINTER(C.c_void_p)
