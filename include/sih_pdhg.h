@@ -135,10 +135,13 @@ typedef struct sih_pdhg_options {
                                   a gathered vector, so that gathers of the longest segments of the other side
                                   skip L2; the step SpMVs then run one 1024-thread block per SM.  0 = automatic
                                   (on where the staged entries carry a large share of the nonzeros), -1 = off */
-    int32_t persistent;        /* mixed: 1 = run the steps between two evaluations as ONE persistent cooperative
-                                  kernel (phases separated by grid barriers with bounded waits; for LPs and batch
-                                  tails whose steps are latency-bound); 0 = one kernel per phase, replayed as CUDA
-                                  graphs (default).  Same iterates either way. */
+    int32_t persistent;        /* mixed: run the steps between two evaluations as ONE persistent cooperative
+                                  kernel, phases separated by grid barriers with bounded waits (for LPs whose
+                                  steps are latency-bound).  1 = the same tasks and reductions as the
+                                  kernel-per-phase path (bit-identical iterates); 2 = for a single LP, static
+                                  task shares with per-block partials reduced by every block (no ticket chain;
+                                  deterministic, equal to the other forms up to rounding; a batch runs form 1).
+                                  0 = one kernel per phase, replayed as CUDA graphs (default). */
 } sih_pdhg_options;
 
 /*

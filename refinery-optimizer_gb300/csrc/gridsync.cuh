@@ -1,19 +1,21 @@
-// Grid-wide barrier of the persistent step kernel, with a bounded wait.
+// Grid-wide barrier of the persistent step kernels, with a bounded wait.
 //
-// The kernel is launched cooperatively (every block resident at once), so a
+// The kernels are launched cooperatively (every block resident at once), so a
 // barrier over all blocks cannot deadlock by itself; the wait is still bounded
 // so that a fault elsewhere can never leave the GPU spinning: a block that
 // waits longer than `limit_ns` (device global timer) sets `status` and
 // returns, and every block that later reaches a barrier (or starts) sees the
 // status and returns too.  The host reads `status` after the launch.
 //
-// Protocol: thread 0 of each block publishes its block's writes (fence),
-// counts itself in `arrive`; the last arriver resets `arrive` and then
-// advances `gen` with a release store; the others poll `gen` with acquire
-// loads.  The fence after the wait makes the other blocks' writes visible to
-// this block's ordinary loads (L1 included); a block barrier then releases the
-// block.  `gen` only grows, and no block can start barrier k + 1 before
-// barrier k completed, so each block can carry the value it expects.
+// Protocol: one 64-bit arrival counter that only grows.  Thread 0 of each
+// block adds 1 with release semantics (after a block barrier, so the block's
+// writes are published with it) and then polls the counter with acquire
+// loads until it reaches the arrivals of this barrier, (k + 1) x expected for
+// the k-th barrier since the counter was zeroed; a block barrier then lets the
+// block's other threads go on (the acquire also makes the other blocks' writes
+// visible to their ordinary loads).  No reset, no second word: the critical
+// path is one atomic and one poll.  The counter is zeroed by the host before
+// each run; a block carries the value it expects next.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -21,8 +23,7 @@
 namespace sihg {
 
 struct GridBar {
-    unsigned* arrive;            // [1] arrivals at the current barrier
-    unsigned* gen;               // [1] completed barriers
+    unsigned long long* count;   // [1] arrivals since the host zeroed it
     int* status;                 // [1] 0 ok, 1 a wait ran out
     unsigned expected;           // blocks that arrive at every barrier (the grid)
     unsigned long long limit_ns; // longest wait of one barrier
@@ -34,14 +35,16 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
-__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ unsigned long long add_release_u64(unsigned long long* p, unsigned long long v) {
+    unsigned long long old;
+    asm volatile("atom.release.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+    return old;
 }
 
 __device__ __forceinline__ int ld_status(const int* p) {
@@ -50,41 +53,40 @@ __device__ __forceinline__ int ld_status(const int* p) {
     return v;
 }
 
-// Value of `gen` when the kernel starts (every block reads the same value: the
-// first barrier cannot complete before all blocks arrived).
-__device__ __forceinline__ unsigned grid_gen(const GridBar& g) { return ld_acquire_u32(g.gen); }
+// Arrivals already counted when the kernel starts, rounded down to whole
+// barriers (every block reads a value below the first barrier's target: that
+// barrier cannot complete before all blocks arrived).
+__device__ __forceinline__ unsigned long long grid_start(const GridBar& g) {
+    const unsigned long long c = ld_acquire_u64(g.count);
+    return c - c % g.expected;
+}
 
 // All blocks of the grid; returns false (uniformly within the block) when a
-// wait ran out here or elsewhere; the caller then returns.
-__device__ __forceinline__ bool grid_barrier(const GridBar& g, unsigned& gen) {
+// wait ran out here or elsewhere; the caller then returns.  `next` holds the
+// counter value this block waits for at its next barrier minus `expected`.
+__device__ __forceinline__ bool grid_barrier(const GridBar& g, unsigned long long& base) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int good = 1;
-        const unsigned target = gen + 1u;
-        __threadfence();
-        if (atomicAdd(g.arrive, 1u) + 1u == g.expected) {
-            *g.arrive = 0u;
-            __threadfence();
-            st_release_u32(g.gen, target);
-        } else {
-            const unsigned long long t0 = global_ns();
-            unsigned spins = 0;
-            while (ld_acquire_u32(g.gen) != target) {
+        const unsigned long long target = base + g.expected;
+        add_release_u64(g.count, 1ull);
+        const unsigned long long t0 = global_ns();
+        unsigned spins = 0;
+        while (ld_acquire_u64(g.count) < target) {
+            if ((++spins & 31u) == 0u) {
                 if (ld_status(g.status) != 0) {
                     good = 0;
                     break;
                 }
-                if ((++spins & 63u) == 0u && global_ns() - t0 > g.limit_ns) {
+                if (global_ns() - t0 > g.limit_ns) {
                     atomicExch(g.status, 1);
                     good = 0;
                     break;
                 }
-                if (spins > 256u) __nanosleep(64);
             }
         }
-        __threadfence();
-        gen = target;
+        base = target;
         ok = good;
     }
     __syncthreads();

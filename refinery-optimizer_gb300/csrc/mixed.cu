@@ -343,7 +343,7 @@ struct KtyStepEpiCoherent : KtyStepEpi {
 __global__ void __launch_bounds__(kThreads, 4)
     k_steps_persistent(int B, int nsteps, Chunks ch, Side rows, Side cols, Vecs V, Inst* st, GridBar gb) {
     if (ld_status(gb.status) != 0) return;  // an earlier launch of this run timed out
-    unsigned gen = grid_gen(gb);
+    unsigned long long gen = grid_start(gb);
     for (int k = 0; k < nsteps; ++k) {
         step_primal_body<2>(ch, V, st);
         if (!grid_barrier(gb, gen)) return;
@@ -361,11 +361,177 @@ __global__ void __launch_bounds__(kThreads, 4)
     }
 }
 
+// ---------------------------------------------------------------- single-LP persistent form
+// For one LP whose steps are latency-bound (every phase a few microseconds of
+// dependent loads), the ticket chain of the task engine (task slot -> group
+// slot -> instance total on the last warp -> controller) is most of a phase.
+// This form (options.persistent = 2, B == 1) keeps the tasks but assigns them
+// statically (warp w takes tasks w, w + warps, ...), so each warp sums its
+// lanes' compensated partials over all its tasks; the block reduces its warps
+// in warp order and stores one partial per block; after the grid barrier
+// EVERY block reduces the block partials in block order and runs the step
+// controller on its own shared-memory copy of the instance state.  The copies
+// stay identical (same data, same operations), so no broadcast and no extra
+// barrier is needed; block 0 writes the state back when the launch ends.
+// Deterministic; the sums are grouped differently from the task engine's, so
+// the iterates agree with the other forms to rounding, not bit for bit.
+constexpr int kSoloThreads = 768;
+
+template <int Q>
+__device__ __forceinline__ void solo_block_partial(Acc (&q)[Q], float2* __restrict__ out, Acc* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    warp_reduce_acc<Q>(q, 0u);
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < Q; ++i) sh[warp * Q + i] = q[i];
+    __syncthreads();
+    if (warp == 0) {
+        Acc v[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            v[i].reset();
+            if (lane < nwarps) v[i] = sh[lane * Q + i];
+        }
+        warp_reduce_acc<Q>(v, 0u);
+        if (lane == 0)
+#pragma unroll
+            for (int i = 0; i < Q; ++i) out[i] = make_float2(v[i].s, v[i].c);
+    }
+}
+
+// Totals of the P block partials (every block computes the same values);
+// valid in thread 0.
+template <int Q>
+__device__ __forceinline__ void solo_grid_total(const float2* __restrict__ part, int P, double (&tot)[Q], Acc* sh) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    Acc v[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) v[i].reset();
+    for (int b = threadIdx.x; b < P; b += blockDim.x)
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const float2 w = __ldcg(part + (size_t)b * Q + i);
+            Acc a;
+            a.s = w.x;
+            a.c = w.y;
+            v[i] = acc_plus(v[i], a);
+        }
+    warp_reduce_acc<Q>(v, 0u);
+    __syncthreads();  // sh is free again (the block partial is stored)
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < Q; ++i) sh[warp * Q + i] = v[i];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            v[i].reset();
+            if (lane < nwarps) v[i] = sh[lane * Q + i];
+        }
+        warp_reduce_acc<Q>(v, 0u);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) tot[i] = (double)v[i].s + (double)v[i].c;
+    }
+}
+
+// This warp's static share of a side's tasks with epilogue `epi`; the lanes'
+// partials (over all the warp's tasks) end in q.
+template <int Q, class Epi>
+__device__ __forceinline__ void solo_side(const Side& side, const Inst& S, Epi& epi, Acc (&q)[Q]) {
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    const int lmax = side.light_max[0];
+    epi.begin(S);
+    for (int ti = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ti < side.ntasks; ti += nw) {
+        const Task t = side.tasks[ti];
+        if (S.refine)
+            run_any_task<1, true>(side, t, lmax, epi);
+        else
+            run_any_task<1, false>(side, t, lmax, epi);
+    }
+    epi.values(q);
+}
+
+__global__ void __launch_bounds__(kSoloThreads, 1)
+    k_solo_steps(int nsteps, int N, int M, Side rows, Side cols, Vecs V, Inst* st, GridBar gb, float2* part) {
+    __shared__ Inst S;
+    __shared__ StepScalars sc;
+    __shared__ Acc red[(kSoloThreads / 32) * 2];
+    if (ld_status(gb.status) != 0) return;
+    if (threadIdx.x == 0) {
+        S = st[0];
+        sc = step_scalars(S);
+    }
+    unsigned long long gen = grid_start(gb);
+    __syncthreads();
+    const int P = gridDim.x;
+    float2* part_rows = part;          // [P] dy2
+    float2* part_cols = part + 2 * P;  // [P][2] inter, dx2
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    for (int k = 0; k < nsteps && !S.done; ++k) {
+        // phase 1: pending average update, x' = clip(x - tau (c + K^T y), l, u)
+        {
+            const StepScalars s = sc;
+            const float* xs = pick(V.x0, V.x1, s.cur);
+            const float* kt = pick(V.kty0, V.kty1, s.cur);
+            float* xn = pick(V.x0, V.x1, s.cur ^ 1);
+            for (int j = tid; j < N; j += nthreads) {
+                const float xv = xs[j];
+                if (s.avg) V.x_acc[j] = ff_axpy(V.x_acc[j], s.w, xv);
+                const float v = fmaf(-s.tau, V.c[j] + kt[j], xv);
+                xn[j] = fminf(fmaxf(v, V.l[j]), V.u[j]);
+            }
+            if (s.avg) {
+                const float* ys = pick(V.y0, V.y1, s.cur);
+                for (int i = tid; i < M; i += nthreads) V.y_acc[i] = ff_axpy(V.y_acc[i], s.w, ys[i]);
+            }
+            // the step-size schedule of this attempt, for the controller at the end of phase 3
+            if (threadIdx.x == blockDim.x - 32) {
+                const double kk = (double)(S.attempts + 2);
+                S.pow06 = pow(kk, -0.6);
+                S.pow03 = pow(kk, -0.3);
+            }
+        }
+        if (!grid_barrier(gb, gen)) return;
+        // phase 2: K x' and the dual step; sum |dy|^2
+        {
+            DualStepEpiCoherent epi{{V}};
+            Acc q[1];
+            solo_side<1>(rows, S, epi, q);
+            solo_block_partial<1>(q, part_rows + blockIdx.x, red);
+        }
+        if (!grid_barrier(gb, gen)) return;
+        {
+            double tot[1];
+            solo_grid_total<1>(part_rows, P, tot, red);
+            if (threadIdx.x == 0) S.dy2 = tot[0];
+            __syncthreads();
+        }
+        // phase 3: K^T y', interaction and movement terms, step controller
+        {
+            KtyStepEpiCoherent epi{{V}};
+            Acc q[2];
+            solo_side<2>(cols, S, epi, q);
+            solo_block_partial<2>(q, part_cols + 2 * blockIdx.x, red);
+        }
+        if (!grid_barrier(gb, gen)) return;
+        {
+            double tot[2];
+            solo_grid_total<2>(part_cols, P, tot, red);
+            if (threadIdx.x == 0) {
+                step_controller(S, tot[1], tot[0]);
+                sc = step_scalars(S);
+            }
+            __syncthreads();
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) st[0] = S;
+}
+
 // Barrier self-test (sih_pdhg_check_grid_barrier): `rounds` grid barriers;
 // with gb.expected above the grid no barrier completes and every block's
 // bounded wait runs out.
 __global__ void k_barrier_probe(GridBar gb, int rounds, unsigned* passed) {
-    unsigned gen = grid_gen(gb);
+    unsigned long long gen = grid_start(gb);
     for (int r = 0; r < rounds; ++r) {
         if (!grid_barrier(gb, gen)) return;
         if (threadIdx.x == 0) atomicAdd(passed, 1u);
@@ -1332,11 +1498,17 @@ int MixedSolver::setup_persistent() {
     SIHG_CUDA(cudaGetDevice(&dev));
     SIHG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) return fail(SIH_PDHG_ERR_UNSUPPORTED, "options.persistent: the device has no cooperative launch");
-    SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_steps_persistent, kThreads, 0));
+    // the single-LP form where it applies (options.persistent = 2, one instance)
+    const bool solo = opts_.persistent == 2 && B_ == 1;
+    if (solo)
+        SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solo_steps, kSoloThreads, 0));
+    else
+        SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_steps_persistent, kThreads, 0));
     if (occ < 1) return fail(SIH_PDHG_ERR_UNSUPPORTED, "options.persistent: the step kernel does not fit on an SM");
     pgrid_ = sm_count_ * occ;
     SIHG_TRY(bar_.alloc(4 * sizeof(unsigned)));
-    persistent_ = 1;
+    if (solo) SIHG_TRY(part_.alloc(sizeof(float2) * 4 * (size_t)pgrid_));
+    persistent_ = solo ? 2 : 1;
     return SIH_PDHG_OK;
 }
 
@@ -1345,10 +1517,10 @@ int MixedSolver::setup_persistent() {
 // a block stopped arriving.
 constexpr double kBarrierLimitSec = 2.0;
 
+// Barrier words: a 64-bit arrival counter, then the status word.
 static GridBar make_bar(const DevMem& words, unsigned expected, double limit_sec) {
-    unsigned* w = words.as<unsigned>();
-    return GridBar{w, w + 1, reinterpret_cast<int*>(w + 2), expected,
-                   (unsigned long long)(limit_sec * 1e9)};
+    unsigned long long* w = words.as<unsigned long long>();
+    return GridBar{w, reinterpret_cast<int*>(w + 1), expected, (unsigned long long)(limit_sec * 1e9)};
 }
 
 // One cooperative launch of the persistent step kernel: `nsteps` steps.
@@ -1363,8 +1535,14 @@ int MixedSolver::launch_persistent(cudaStream_t s, int nsteps) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     const GridBar gb = make_bar(bar_, (unsigned)pgrid_, kBarrierLimitSec);
-    SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_steps_persistent, B_, nsteps, chunks_all_, rows_, cols_, V_,
-                                 state_.as<Inst>(), gb));
+    if (persistent_ == 2) {
+        cfg.blockDim = dim3((unsigned)kSoloThreads);
+        SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_solo_steps, nsteps, N_, M_, rows_, cols_, V_, state_.as<Inst>(), gb,
+                                     part_.as<float2>()));
+    } else {
+        SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_steps_persistent, B_, nsteps, chunks_all_, rows_, cols_, V_,
+                                     state_.as<Inst>(), gb));
+    }
     launches_ += 1;
     return SIH_PDHG_OK;
 }
@@ -1390,12 +1568,12 @@ int check_grid_barrier(int blocks, int missing, int rounds, double limit_sec, in
     cfg.blockDim = dim3((unsigned)kThreads);
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_barrier_probe, gb, rounds, words.as<unsigned>() + 4));
+    SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_barrier_probe, gb, rounds, words.as<unsigned>() + 6));
     SIHG_CUDA(cudaDeviceSynchronize());
     unsigned h[8];
     SIHG_CUDA(cudaMemcpy(h, words.as<void>(), sizeof(h), cudaMemcpyDeviceToHost));
     if (timed_out) *timed_out = (int)h[2];
-    if (passed) *passed = (int)(h[4] / (unsigned)blocks);
+    if (passed) *passed = (int)(h[6] / (unsigned)blocks);
     return SIH_PDHG_OK;
 }
 
@@ -1644,7 +1822,7 @@ int MixedSolver::run() {
     if (rc != SIH_PDHG_OK) return rc;
     if (persistent_) {
         int status = 0;
-        SIHG_CUDA(cudaMemcpy(&status, bar_.as<unsigned>() + 2, sizeof(int), cudaMemcpyDeviceToHost));
+        SIHG_CUDA(cudaMemcpy(&status, bar_.as<unsigned long long>() + 1, sizeof(int), cudaMemcpyDeviceToHost));
         if (status != 0)
             return fail(SIH_PDHG_ERR_CUDA, "persistent step kernel: a grid barrier wait ran out (a block stopped "
                                            "arriving); the solve was abandoned");

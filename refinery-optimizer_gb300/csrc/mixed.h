@@ -207,8 +207,9 @@ class MixedSolver {
     int stage_x_ = 0, stage_y_ = 0;
     // persistent step kernel (options.persistent): its grid (every block
     // resident) and the grid barrier's words {arrive, gen, status}
+    // (1 = the task-engine form, 2 = the single-LP form with per-block partials)
     int persistent_ = 0, pgrid_ = 0;
-    DevMem bar_;
+    DevMem bar_, part_;
     Vecs V_{};
     std::vector<Inst> host_inst_;
     std::vector<std::vector<float>> start_x_, start_y_;  // warm starts (device order, unscaled)

@@ -87,3 +87,32 @@ def test_grid_barrier_wait_runs_out_and_the_device_stays_usable(sih):
     assert time.perf_counter() - t0 < 5.0
     prob, _, _ = golden_case("rand_200x500_k8_s0")
     assert sih.solve_gpu_mixed(prob, cfg(sih), persistent=1).is_optimal()
+
+
+@pytest.mark.parametrize("name", ["rand_200x500_k8_s0", "rand_2000x5000_k8_s0", "toy04_lp_equality_ranges"])
+def test_single_lp_persistent_form_solves_like_the_graph_path(sih, name):
+    """options.persistent = 2: static task shares and per-block partials give
+    other roundings than the ticket chain, so the trajectory may differ in the
+    last bits: same status, tolerance reached, the same optimum."""
+    prob, entry, _ = golden_case(name)
+    a = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6))
+    b = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6), persistent=2)
+    assert a.is_optimal() and b.is_optimal()
+    assert max(b.rel_primal, b.rel_dual, b.rel_gap) <= 2e-6
+    assert abs(b.simplex_iterations - a.simplex_iterations) <= max(4 * 64, 0.2 * a.simplex_iterations)
+    ref = entry["highs_objective"]
+    assert abs(b.primal_objective - ref) <= 4e-6 * (1 + abs(ref))
+
+
+def test_single_lp_persistent_form_is_deterministic(sih):
+    from sih_pdhg.generators import refinery_lp
+
+    prob = refinery_lp(24, 2)
+    with sih.PdhgHandle(prob, cfg(sih), algorithm=sih.ALGO_MIXED, persistent=2) as h:
+        h.run()
+        a = h.result(0)
+        h.run()
+        b = h.result(0)
+    assert a.is_optimal() and a.simplex_iterations == b.simplex_iterations
+    np.testing.assert_array_equal(a.x, b.x)
+    np.testing.assert_array_equal(a.row_duals, b.row_duals)
