@@ -26,8 +26,10 @@ Workloads (seeded synthetic LPs, FP64 data, generators in sih_pdhg.generators):
   mps:PATH       the LP of an MPS file (sih_pdhg.read_mps); the reference arm prints
                  an `unavailable` line for it (no measured plain iteration count)
 
-Multi-GPU: replicas (each rank solves its own copy of a single LP, or its own
-seeded batch of a batch workload; no data-path exchange; scaling "weak").
+Multi-GPU: a single LP is replicated (each rank solves its own copy; scaling
+"weak"); a batch workload is partitioned by instance (rank r solves instances
+r, r + N, ...; the per-instance results are gathered on the host; scaling
+"strong": the whole batch is the job).  No data-path exchange either way.
 --impl reference times the reference's algorithm (plain FP32 PDHG) through its
 CPU port (oracle/pdhg_oracle.c, OpenMP over all host threads): every timed
 step is one complete solve of the workload LP from the initial point until the
@@ -75,6 +77,16 @@ NCU_TRAFFIC_PER_LAUNCH = {
 }
 
 
+# Engine options a workload runs with beyond the defaults (reported in the line's
+# config): the refinery scenario batches use primal-weight smoothing 0.8, which
+# took 358 s for the 512-scenario batch against 441 s with PDLP's 0.5 (the
+# slowest scenarios follow the primal weight much better; the single 168-period
+# LP is faster with 0.5, 11,904 against 15,232 steps).
+WORKLOAD_OPTIONS = {
+    "refinery-512": {"primal_weight_smoothing": 0.8},
+    "refinery-64": {"primal_weight_smoothing": 0.8},
+}
+
 WORKLOADS = ["zipf-500kx1m", "random-2kx5k", "refinery-168p", "refinery-512", "refinery-64", "random-2kx5k-x256"]
 
 
@@ -116,7 +128,11 @@ def parse_args():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tol", type=float, default=1e-4)
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
-    ap.add_argument("--plain-sample", type=int, default=4,
+    ap.add_argument("--persistent", type=int, default=-1,
+                    help="options.persistent of the engine (step form): -1 automatic, 0 graphs, 1 / 2 persistent")
+    ap.add_argument("--highs-seconds", type=float, default=60.0,
+                    help="single LPs: time limit of the HiGHS IPM baseline on the host cores (0 = skip)")
+    ap.add_argument("--plain-sample", type=int, default=8,
                     help="batch workloads: scenarios timed with the plain algorithm for the sequential estimate")
     ap.add_argument("--plain-cap", type=int, default=1_000_000,
                     help="batch workloads: iteration cap of those plain solves")
@@ -138,16 +154,33 @@ def run_profile_solve(args) -> None:
     prob = make_workload(args.workload, seed=0)
     cfg = sih_pdhg.GpuPdhgConfig(max_iterations=args.profile_solve, tol_primal=1e-12, tol_dual=1e-12, tol_gap=1e-12)
     algo = sih_pdhg.ALGO_MIXED if args.profile_algorithm == "mixed" else sih_pdhg.ALGO_PLAIN
-    sol = sih_pdhg.GpuSolver.solve_ex(prob, cfg, algorithm=algo, use_graph=0)
+    sol = sih_pdhg.GpuSolver.solve_ex(prob, cfg, algorithm=algo, use_graph=0, persistent=args.persistent)
     print(f"profile solve: {sol.simplex_iterations} steps, {sol.time_solver_sec * 1e3:.2f} ms device time")
 
 
 def workload_seed(name: str, rank: int) -> int:
-    """Replicas: every rank solves the same single LP (seed 0); for a batch
-    workload each rank solves its own seeded batch of the same size (per-GPU
-    work fixed, no data-path exchange: weak scaling)."""
-    batch = name in ("refinery-512", "refinery-64", "random-2kx5k-x256")
-    return rank if batch else 0
+    """Every rank builds the same workload (seed 0): a single LP is solved by
+    every rank (replicas), a batch is partitioned by instance (shard)."""
+    return 0
+
+
+def shard(items, rank: int, world: int):
+    """Instances of a batch for one rank: rank, rank + world, ... (strided, so
+    every rank gets a like mix of scenario sizes); with their batch indices."""
+    idx = list(range(rank, len(items), world))
+    return [items[i] for i in idx], idx
+
+
+def gather_instances(rows, world: int):
+    """Host gather of the per-instance summaries of every rank's shard (the only
+    exchange of the partitioned batch): every rank gets all rows in batch order."""
+    if world == 1:
+        return sorted(rows, key=lambda r: r["index"])
+    import torch.distributed as dist
+
+    parts = [None] * world
+    dist.all_gather_object(parts, rows)
+    return sorted((r for part in parts for r in part), key=lambda r: r["index"])
 
 
 def reduce_max(v: float, world: int, device: str) -> float:
@@ -160,6 +193,18 @@ def reduce_max(v: float, world: int, device: str) -> float:
     t = torch.tensor([v], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def reduce_sum(vals, world: int, device: str):
+    """Element-wise sum of per-rank floats over the process group."""
+    if world == 1:
+        return list(vals)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor(list(vals), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return [float(v) for v in t.tolist()]
 
 
 def dist_env():
@@ -241,6 +286,66 @@ def cpu_pdlp_sample(problem, gpu_attempts: int, sample_s: float) -> dict:
     return {"value": per_step * gpu_attempts, "unit": "s", "cores": os.cpu_count() or 1, "kind": "port",
             "sample": f"{attempts} steps of the FP64 CPU port of the same algorithm ({dt:.1f} s), "
                       f"scaled to the {gpu_attempts} steps the GPU needed"}
+
+
+def _highs_child(path: str, conn) -> None:
+    """Child process of cpu_highs: solve the LP stored at `path` with scipy HiGHS IPM."""
+    import numpy as np
+    import scipy.sparse as sp
+    from scipy.optimize import linprog
+
+    d = np.load(path)
+    A = sp.csc_matrix((d["val"], d["ri"], d["cp"]), shape=(int(d["m"]), int(d["n"])))
+    rl, ru = d["rl"], d["ru"]
+    eq = rl == ru
+    ub = (~eq) & np.isfinite(ru)
+    lb = (~eq) & np.isfinite(rl)
+    bounds = [(a if np.isfinite(a) else None, b if np.isfinite(b) else None) for a, b in zip(d["cl"], d["cu"])]
+    t0 = time.perf_counter()
+    r = linprog(d["c"], A_ub=sp.vstack([A[ub], -A[lb]]).tocsc(), b_ub=np.concatenate([ru[ub], -rl[lb]]),
+                A_eq=A[eq].tocsc(), b_eq=rl[eq], bounds=bounds, method="highs-ipm")
+    conn.send((int(r.status), float(r.fun) if r.status == 0 else None, time.perf_counter() - t0))
+
+
+def cpu_highs(prob, limit_s: float) -> dict:
+    """HiGHS interior point (scipy's linprog, method 'highs-ipm') on the same LP on
+    this host's cores: the FP64 solver listed as a CPU baseline for context.  It
+    runs in a child process that is stopped after limit_s seconds (HiGHS's own
+    time limit is not checked inside a factorisation); a stopped run is
+    reported as not finished."""
+    import multiprocessing as mp
+
+    import numpy as np
+
+    try:
+        import scipy  # noqa: F401
+    except ImportError:
+        return {"value": None, "unit": "s", "finished": False, "sample": "scipy not installed on this host"}
+    p = prob
+    sign = 1 if int(p.sense) == 1 else -1
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "lp.npz")
+        np.savez(path, m=p.num_rows(), n=p.num_cols(), cp=p.A.csc_col_ptr(), ri=p.A.csc_row_ind(),
+                 val=p.A.csc_values(), c=p.c * sign, cl=p.col_lower, cu=p.col_upper, rl=p.row_lower, ru=p.row_upper)
+        ctx = mp.get_context("spawn")  # no fork of a process that holds a CUDA context
+        recv, send = ctx.Pipe(duplex=False)
+        child = ctx.Process(target=_highs_child, args=(path, send))
+        child.start()
+        res, t_end = None, time.perf_counter() + limit_s
+        while time.perf_counter() < t_end:
+            if recv.poll(0.25):
+                res = recv.recv()
+                break
+            if not child.is_alive():
+                break
+        if child.is_alive():
+            child.terminate()  # this child only
+        child.join(10)
+    done = res is not None and res[0] == 0
+    return {"value": res[2] if done else None, "unit": "s", "finished": done, "cores": os.cpu_count() or 1,
+            "objective": res[1] * sign if done else None,
+            "sample": (f"scipy HiGHS IPM on the same LP in a child process, stopped after {limit_s:g} s: "
+                       + (f"optimal in {res[2]:.2f} s" if done else "did not finish"))}
 
 
 def cpu_plain_per_iteration(data, iters: int, threads: int) -> float:
@@ -348,11 +453,14 @@ def run_gb300(args) -> None:
         return reduce_max(v, world, "cuda")
 
     work = make_workload(args.workload, seed=workload_seed(args.workload, rank))
-    probs = as_list(work)
     batch = isinstance(work, list)
+    all_probs = as_list(work)
+    # a batch is partitioned by instance over the ranks; a single LP is replicated
+    probs, my_index = shard(all_probs, rank, world) if batch else (all_probs, [0])
     tol = args.tol
     cfg = sih_pdhg.GpuPdhgConfig(max_iterations=1_000_000, tol_primal=tol, tol_dual=tol, tol_gap=tol)
-    handle = sih_pdhg.PdhgHandle(probs, cfg, algorithm=sih_pdhg.ALGO_MIXED)
+    wopts = WORKLOAD_OPTIONS.get(args.workload, {})
+    handle = sih_pdhg.PdhgHandle(probs, cfg, algorithm=sih_pdhg.ALGO_MIXED, persistent=args.persistent, **wopts)
     for _ in range(args.warmup):
         handle.run()
     barrier()
@@ -367,7 +475,10 @@ def run_gb300(args) -> None:
     sols = [handle.result(i) for i in range(len(probs))]
     step = max_over_ranks(statistics.mean(times))
     launches = sols[0].kernel_launches * args.steps
-    iters = [s.simplex_iterations for s in sols]
+    rows = gather_instances([{"index": i, "status": int(s.status), "iterations": int(s.simplex_iterations),
+                              "rel": [s.rel_primal, s.rel_dual, s.rel_gap], "objective": s.primal_objective}
+                             for i, s in zip(my_index, sols)], world if batch else 1)
+    iters = [r["iterations"] for r in rows]
 
     # roofline of the dominant SpMV kernel (live CUDA-event timing on the solver stream)
     secs, byts = handle.time_kernels(20)
@@ -376,6 +487,7 @@ def run_gb300(args) -> None:
     peak, peak_src = measured_hbm_peak()
     achieved = byts[dom] / secs[dom] / 1e9
     all_gbs = {names[k]: round(byts[k] / secs[k] / 1e9, 1) for k in range(3)}
+    shape = handle.launch_shape()
     handle.close()
 
     # end to end through the C ABI with host buffers (upload .. download inside)
@@ -384,32 +496,39 @@ def run_gb300(args) -> None:
     for i in range(1 if batch else 2):
         barrier()
         t0 = time.perf_counter()
-        e2e_sols = sih_pdhg.solve_batch(probs, cfg) if batch else [sih_pdhg.solve_gpu_mixed(probs[0], cfg)]
+        e2e_sols = (sih_pdhg.solve_batch(probs, cfg, persistent=args.persistent, **wopts) if batch
+                    else [sih_pdhg.solve_gpu_mixed(probs[0], cfg, persistent=args.persistent, **wopts)])
         torch.cuda.synchronize()
         if batch or i > 0 or args.steps <= 1:
             e2e_times.append(time.perf_counter() - t0)
     e2e = max_over_ranks(statistics.mean(e2e_times))
     h2d = sum(int(s.h2d_bytes) for s in e2e_sols)  # per instance: matrix, vectors
     d2h = sum(int(s.d2h_bytes) for s in e2e_sols)
+    if batch and world > 1:  # the whole job's bytes: every rank moved its shard
+        h2d, d2h = (int(v) for v in reduce_sum([float(h2d), float(d2h)], world, "cuda"))
 
     if rank != 0:
         return
-    cfg_desc = workload_config(args.workload, probs, tol)
+    cfg_desc = workload_config(args.workload, all_probs, tol)
     line = {
         "metric": METRIC, "value": step, "unit": "s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": False, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": False,
+        "scaling": "strong" if batch and world > 1 else "weak",
         "vs_baseline": None, "dtype": "f32+f64",
         "data": (f"MPS file {args.workload[4:]}" if args.workload.startswith("mps:")
                  else "synthetic (seeded generator, seed 0)"),
         "config": cfg_desc,
-        "algorithm": "mixed-precision restarted adaptive PDHG", "parallelism": f"replicas x{world}",
+        "algorithm": "mixed-precision restarted adaptive PDHG",
+        "parallelism": (f"instance partition x{world}" if batch and world > 1 else f"replicas x{world}"),
         "iterations": max(iters), "restarts": sols[0].restarts,
-        "status": max(int(s.status) for s in sols),
-        "rel_kkt": [max(s.rel_primal for s in sols), max(s.rel_dual for s in sols), max(s.rel_gap for s in sols)],
+        "status": max(r["status"] for r in rows),
+        "rel_kkt": [max(r["rel"][k] for r in rows) for k in range(3)],
         "wall_s_per_step": wall / args.steps,
         "clocks": clock_info,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
+        "launch_shape": shape,
+        "engine_options": wopts,
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_src,
                      "traffic": NCU_TRAFFIC_PER_LAUNCH.get((args.workload, names[dom])),
@@ -422,18 +541,20 @@ def run_gb300(args) -> None:
     if batch:
         line["iterations_per_instance"] = {"min": min(iters), "median": int(statistics.median(iters)),
                                            "max": max(iters)}
-        line["plain_gpu_sequential"] = plain_sequential_sample(probs, tol, args.plain_sample, args.plain_cap)
+        line["plain_gpu_sequential"] = plain_sequential_sample(all_probs, tol, args.plain_sample, args.plain_cap)
     # CPU baseline: the FP64 port of the same algorithm on one instance, scaled
     # to the whole job by nonzero-steps
-    big = max(range(len(probs)), key=lambda i: probs[i].num_nonzeros()) if not batch else 0
-    cb = cpu_pdlp_sample(probs[big], iters[big], args.cpu_sample_seconds)
+    big = 0
+    cb = cpu_pdlp_sample(all_probs[big], iters[big], args.cpu_sample_seconds)
     if batch:
-        work_all = sum(it * p.num_nonzeros() for it, p in zip(iters, probs))
-        scale = work_all / (iters[big] * probs[big].num_nonzeros())
+        work_all = sum(it * p.num_nonzeros() for it, p in zip(iters, all_probs))
+        scale = work_all / (iters[big] * all_probs[big].num_nonzeros())
         cb["value"] *= scale
-        cb["sample"] += (f"; x {scale:.1f} to cover all {len(probs)} instances "
+        cb["sample"] += (f"; x {scale:.1f} to cover all {len(all_probs)} instances "
                          f"(sum over instances of steps x nonzeros)")
     line["cpu_baseline"] = cb
+    if not batch and args.highs_seconds > 0:
+        line["cpu_highs"] = cpu_highs(all_probs[0], args.highs_seconds)
     print(json.dumps(line), flush=True)
 
 

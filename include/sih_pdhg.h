@@ -112,8 +112,11 @@ typedef struct sih_pdhg_options {
     int32_t compensated;       /* mixed: 0 off, 1 on near tolerance (default), 2 always */
     int32_t dual_sign;         /* 0 = PDHG sign of the reference (row_duals = -simplex duals), 1 = simplex sign */
     int32_t use_graph;         /* 1 = replay iteration blocks as CUDA graphs */
-    int32_t autotune;          /* mixed: 1 = time the SpMV task sizes once per batch shape (instances, rows,
-                                  columns, nonzeros) at creation and keep the fastest (cached per process) */
+    int32_t autotune;          /* mixed: 1 = at creation, time the step kernels' launch shapes (task size, lanes
+                                  per segment of each side, staged gathers, and with persistent < 0 the step
+                                  form) on this batch and keep the fastest, once per batch shape (instances,
+                                  rows, columns, nonzeros; cached per process); 0 = off; -1 = on for batches
+                                  of two or more LPs (default) */
     int32_t verbose;           /* 0 */
     double time_limit_sec;     /* <= 0: none */
     double restart_sufficient; /* mixed: 0.2 */
@@ -141,7 +144,9 @@ typedef struct sih_pdhg_options {
                                   kernel-per-phase path (bit-identical iterates); 2 = for a single LP, static
                                   task shares with per-block partials reduced by every block (no ticket chain;
                                   deterministic, equal to the other forms up to rounding; a batch runs form 1).
-                                  0 = one kernel per phase, replayed as CUDA graphs (default). */
+                                  0 = one kernel per phase, replayed as CUDA graphs; -1 = automatic (default):
+                                  form 2 for one LP whose matrix fits in half of L2, the autotuner's choice
+                                  when it runs, else 0. */
 } sih_pdhg_options;
 
 /*
@@ -243,6 +248,21 @@ int sih_pdhg_set_start(sih_pdhg_handle* h, int32_t index, const double* x, const
 /* Nonzeros per SpMV task in use (mixed algorithm; the autotuner's choice with
  * options.autotune = 1). */
 int sih_pdhg_get_task_nnz(const sih_pdhg_handle* h, int32_t* task_nnz);
+
+/* Launch shape of the mixed solver's step kernels: what the autotuner chose
+ * (options.autotune) or the rules gave.  No counterpart in the reference, whose
+ * kernels launch with fixed 256-thread blocks (cuda_pdhg.cu:155-203). */
+typedef struct sih_pdhg_launch_shape {
+    int32_t task_nnz;   /* nonzeros per SpMV task */
+    int32_t row_lanes;  /* lanes per row of the A x light tasks (0 = the length rule) */
+    int32_t col_lanes;  /* lanes per column of the A^T y light tasks (0 = the length rule) */
+    int32_t staged_x;   /* entries of x staged in shared memory for A x (0 = off) */
+    int32_t staged_y;   /* entries of y staged for A^T y (0 = off) */
+    int32_t persistent; /* step form: 0 kernels per phase (graphs), 1 / 2 persistent (options.persistent) */
+    int32_t grid;       /* blocks of the step SpMV launches */
+    int32_t tuned;      /* 1 when the autotuner chose the shape */
+} sih_pdhg_launch_shape;
+int sih_pdhg_get_launch_shape(const sih_pdhg_handle* h, sih_pdhg_launch_shape* shape);
 void sih_pdhg_destroy(sih_pdhg_handle* h);
 
 /* Self-test of the grid barrier of the persistent step kernel
@@ -286,6 +306,20 @@ int sih_pdhg_launch_residuals(int m, int n, const float* d_Ax, const float* d_ro
                               float* d_row_viols, const float* d_x, const float* d_c, const float* d_AT_y,
                               const float* d_l, const float* d_u, const float* d_tau, float* d_col_viols,
                               void* stream);
+
+/* ---- hybrid polish: basis guess on the device ------------------------------
+ * Replaces the host scoring of GpuSolver::solve_hybrid
+ * (core/src/gpu/gpu_solver.cpp:332-395) that feeds SimplexSolver::solve_from_basis:
+ * every column (value x_j) and row (activity row_activity_i = (A x)_i) gets the
+ * distance to its nearer finite bound (bounds beyond +-1e15 count as absent,
+ * distance 1e30); the m candidates with the largest distance are Basic (0),
+ * the others AtLower (1) or AtUpper (2), the nearer bound (AtLower on a tie).
+ * Candidates are columns then rows; equal distances are taken in that order
+ * (a stable descending sort, as the reference's std::sort gives for distinct
+ * distances).  Scoring and top-m selection (radix select) run on the GPU;
+ * host arrays in and out. */
+int sih_pdhg_basis_guess(const sih_pdhg_problem* problem, const double* x, const double* row_activity,
+                         int8_t* col_status, int8_t* row_status);
 
 /* ---- adjoint (differentiation of the LP solution map) ---------------------
  * No counterpart in the reference (its docs/gpu_pdhg.md plans a differentiable

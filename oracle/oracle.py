@@ -234,3 +234,22 @@ def plain_solve_kkt(d, tol: float, eval_every: int = 100, max_iters: int = 1_000
     if rc != 0:
         raise ValueError("oracle_plain_solve_kkt rejected its arguments")
     return dict(iterations=int(out[0]), rel_primal=float(out[1]), rel_dual=float(out[2]), rel_gap=float(out[3]))
+
+
+def basis_guess(problem, x, row_activity):
+    """Basis guess of the reference's hybrid polish (core/src/gpu/gpu_solver.cpp:332-395):
+    distance of every column value / row activity to its nearer finite bound
+    (bounds beyond +-1e15 absent: distance 1e30), the m largest Basic (0), the
+    rest AtLower (1) / AtUpper (2) by the nearer bound (AtLower on a tie); equal
+    distances in candidate order (columns, then rows), i.e. a stable descending
+    sort.  Returns (col_status, row_status) int8 arrays."""
+    n, m = problem.num_cols(), problem.num_rows()
+    v = np.concatenate([np.asarray(x, dtype=np.float64), np.asarray(row_activity, dtype=np.float64)])
+    lo = np.concatenate([problem.col_lower, problem.row_lower]).astype(np.float64)
+    hi = np.concatenate([problem.col_upper, problem.row_upper]).astype(np.float64)
+    dl = np.where(lo > -1e15, np.maximum(0.0, v - lo), 1e30)
+    du = np.where(hi < 1e15, np.maximum(0.0, hi - v), 1e30)
+    d = np.minimum(dl, du)
+    status = np.where(dl <= du, 1, 2).astype(np.int8)
+    status[np.argsort(-d, kind="stable")[:m]] = 0
+    return status[:n], status[n:]

@@ -151,7 +151,8 @@ void sih_pdhg_options_default(sih_pdhg_options* o) {
     o->use_graph = 1;
     o->reorder = 1;
     o->staged_kib = 0;
-    o->autotune = 0;
+    o->autotune = -1;
+    o->persistent = -1;
     o->verbose = 0;
     o->time_limit_sec = 0.0;
     o->restart_sufficient = 0.2;

@@ -150,6 +150,13 @@ int sih_pdhg_get_task_nnz(const sih_pdhg_handle* h, int32_t* task_nnz) {
     return SIH_PDHG_OK;
 }
 
+int sih_pdhg_get_launch_shape(const sih_pdhg_handle* h, sih_pdhg_launch_shape* shape) {
+    if (!h || !shape) return fail(SIH_PDHG_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!h->mixed) return fail(SIH_PDHG_ERR_UNSUPPORTED, "launch shapes belong to the mixed algorithm");
+    h->mixed->launch_shape(shape);
+    return SIH_PDHG_OK;
+}
+
 void sih_pdhg_destroy(sih_pdhg_handle* h) { delete h; }
 
 int sih_pdhg_check_grid_barrier(int32_t blocks, int32_t missing, int32_t rounds, double limit_sec,

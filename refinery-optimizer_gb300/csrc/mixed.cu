@@ -167,19 +167,38 @@ __global__ void __launch_bounds__(kThreads) k_step_primal(int B, Chunks ch, Vecs
     step_primal_body<4>(ch, V, st);
 }
 
-// The step-size schedule factors k^-0.6 and k^-0.3 of this attempt (k =
-// attempts + 2) for the controller at the end of the A^T y kernel.  FP64 pow
-// is slow on this part: thread 0 of block b computes instances b, b + grid,
-// ... at the start of the A x kernel, whose other warps meanwhile take the
-// tasks (a kernel of this length hides it; the elementwise pass did not).
-__device__ __forceinline__ void step_schedule_pows(int B, Inst* __restrict__ st) {
+// The step-size schedule factors k^-0.6 and k^-0.3 of attempt k (k =
+// attempts + 2).  FP64 pow is slow on this part (a chain of FP64 operations on
+// a pipe that issues two per SM per clock), so the set-up tabulates both for
+// every k the iteration limit reaches (up to kPowTable entries; beyond, pow
+// runs on the device as before); the table holds the same pow results.
+constexpr int kPowTable = 1 << 20;
+
+__global__ void k_pow_table(int n, double2* __restrict__ tab) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        tab[k] = make_double2(pow((double)k, -0.6), pow((double)k, -0.3));
+}
+
+__device__ __forceinline__ void schedule_pows(Inst& S, const Vecs& V) {
+    const long long k = S.attempts + 2;
+    if (k < V.pow_n) {
+        const double2 p = V.pow_tab[k];
+        S.pow06 = p.x;
+        S.pow03 = p.y;
+    } else {
+        S.pow06 = pow((double)k, -0.6);
+        S.pow03 = pow((double)k, -0.3);
+    }
+}
+
+// Thread 0 of block b loads the factors of instances b, b + grid, ... at the
+// start of the A x kernel for the controller at the end of the A^T y kernel.
+__device__ __forceinline__ void step_schedule_pows(int B, Inst* __restrict__ st, const Vecs& V) {
     if (threadIdx.x != 0) return;
     for (int b = blockIdx.x; b < B; b += gridDim.x) {
         Inst& S = st[b];
         if (S.done) continue;
-        const double k = (double)(S.attempts + 2);
-        S.pow06 = pow(k, -0.6);
-        S.pow03 = pow(k, -0.3);
+        schedule_pows(S, V);
     }
 }
 
@@ -220,7 +239,7 @@ struct DualStepEpi {
 
 __global__ void __launch_bounds__(kThreads, 4) k_step_dual(int B, Side rows, Vecs V, Inst* __restrict__ st) {
     chain_wait();
-    step_schedule_pows(B, st);
+    step_schedule_pows(B, st, V);
     DualStepEpi epi{V};
     spmv_engine<1, true, 1>(rows, st, epi, 0u);
 }
@@ -313,7 +332,7 @@ __global__ void __launch_bounds__(kStagedThreads, 1)
     k_step_dual_staged(int B, Side rows, Vecs V, Inst* __restrict__ st, int staged) {
     chain_wait();
     stage_prefix(pick(V.x0, V.x1, st[0].cur ^ 1), staged);
-    step_schedule_pows(B, st);
+    step_schedule_pows(B, st, V);
     DualStepEpiStaged epi{{V}, staged};
     spmv_engine<1, true, 1>(rows, st, epi, 0u);
 }
@@ -347,7 +366,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     for (int k = 0; k < nsteps; ++k) {
         step_primal_body<2>(ch, V, st);
         if (!grid_barrier(gb, gen)) return;
-        step_schedule_pows(B, st);
+        step_schedule_pows(B, st, V);
         {
             DualStepEpiCoherent epi{{V}};
             spmv_engine<1, true, 1>(rows, st, epi, 0u);
@@ -376,6 +395,10 @@ __global__ void __launch_bounds__(kThreads, 4)
 // Deterministic; the sums are grouped differently from the task engine's, so
 // the iterates agree with the other forms to rounding, not bit for bit.
 constexpr int kSoloThreads = 768;
+// Automatic step form: the single-LP form when the matrix (both sides) takes
+// at most this many bytes, half of the 129 MB L2 (measured per step: 80k
+// nonzeros 30.9 -> 20.8 us, 1.1M nonzeros 46.1 -> 38.8 us).
+constexpr double kSoloMaxBytes = 64.0 * 1024.0 * 1024.0;
 
 template <int Q>
 __device__ __forceinline__ void solo_block_partial(Acc (&q)[Q], float2* __restrict__ out, Acc* sh) {
@@ -485,11 +508,7 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
                 for (int i = tid; i < M; i += nthreads) V.y_acc[i] = ff_axpy(V.y_acc[i], s.w, ys[i]);
             }
             // the step-size schedule of this attempt, for the controller at the end of phase 3
-            if (threadIdx.x == blockDim.x - 32) {
-                const double kk = (double)(S.attempts + 2);
-                S.pow06 = pow(kk, -0.6);
-                S.pow03 = pow(kk, -0.3);
-            }
+            if (threadIdx.x == blockDim.x - 32) schedule_pows(S, V);
         }
         if (!grid_barrier(gb, gen)) return;
         // phase 2: K x' and the dual step; sum |dy|^2
@@ -1236,10 +1255,14 @@ static int upload(DevMem& d, const void* h, size_t bytes, cudaStream_t s) {
 // tasks of about `task_nnz` nonzeros (rebuilt by the autotuner).
 int MixedSolver::build_schedules(int task_nnz) {
     task_nnz_ = task_nnz;
+    if (graphs_[0]) {  // the recorded graph holds the old schedules
+        cudaGraphExecDestroy(graphs_[0]);
+        graphs_[0] = nullptr;
+    }
     SIHG_TRY(layout_.build(h_csr_ptr_, h_csc_ptr_, row_off_, col_off_,
                            SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()},
                            SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, task_nnz_, false, stream_,
-                           opts_.lanes_csr, opts_.lanes_csc));
+                           lanes_r_, lanes_c_));
     rows_ = layout_.rows;
     cols_ = layout_.cols;
     chunks_all_ = layout_.chunks;
@@ -1406,6 +1429,8 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     }
     h_csr_ptr_ = std::move(csr_ptr);
     h_csc_ptr_ = std::move(csc_ptr);
+    lanes_r_ = opts.lanes_csr;
+    lanes_c_ = opts.lanes_csc;
     SIHG_TRY(build_schedules(task_nnz_));
     SIHG_TRY(choose_staging());
 
@@ -1482,9 +1507,19 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
         S.beta_art = opts.restart_artificial;
         S.weight_smoothing = opts.primal_weight_smoothing;
     }
+    {
+        const long long need = (long long)cfg.max_iterations + 3;
+        const int n = (int)std::max(3LL, std::min<long long>(need, kPowTable));
+        SIHG_TRY(pow_tab_.alloc(sizeof(double2) * (size_t)n));
+        k_pow_table<<<std::max(1, std::min(sm_count_ * 4, (n + 255) / 256)), 256, 0, s>>>(n, pow_tab_.as<double2>());
+        SIHG_LAUNCH_CHECK();
+        V_.pow_tab = pow_tab_.as<double2>();
+        V_.pow_n = n;
+    }
     phase("state");
-    if (opts.autotune && opts.tile_nnz <= 0) SIHG_TRY(autotune());
     SIHG_TRY(setup_persistent());
+    // autotune: 1 on, 0 off, < 0 automatic (on for batches)
+    if (opts.autotune > 0 || (opts.autotune < 0 && B_ > 1)) SIHG_TRY(autotune());
     return SIH_PDHG_OK;
 }
 
@@ -1493,22 +1528,39 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
 // kernel's occupancy; the barrier words are reset at the start of each run.
 int MixedSolver::setup_persistent() {
     persistent_ = 0;
-    if (opts_.persistent == 0) return SIH_PDHG_OK;
+    grid_form1_ = grid_form2_ = 0;
     int dev = 0, coop = 0, occ = 0;
     SIHG_CUDA(cudaGetDevice(&dev));
     SIHG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-    if (!coop) return fail(SIH_PDHG_ERR_UNSUPPORTED, "options.persistent: the device has no cooperative launch");
-    // the single-LP form where it applies (options.persistent = 2, one instance)
-    const bool solo = opts_.persistent == 2 && B_ == 1;
-    if (solo)
-        SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solo_steps, kSoloThreads, 0));
-    else
+    if (coop) {
         SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_steps_persistent, kThreads, 0));
-    if (occ < 1) return fail(SIH_PDHG_ERR_UNSUPPORTED, "options.persistent: the step kernel does not fit on an SM");
-    pgrid_ = sm_count_ * occ;
-    SIHG_TRY(bar_.alloc(4 * sizeof(unsigned)));
-    if (solo) SIHG_TRY(part_.alloc(sizeof(float2) * 4 * (size_t)pgrid_));
-    persistent_ = solo ? 2 : 1;
+        grid_form1_ = sm_count_ * occ;
+        if (B_ == 1) {
+            SIHG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solo_steps, kSoloThreads, 0));
+            grid_form2_ = sm_count_ * occ;
+        }
+        SIHG_TRY(bar_.alloc(4 * sizeof(unsigned)));
+        SIHG_TRY(part_.alloc(sizeof(float2) * 4 * (size_t)std::max(1, grid_form2_)));
+    }
+    int form = opts_.persistent;
+    if (form < 0) {
+        // automatic: the single-LP form for one LP whose matrix (both sides,
+        // 16 bytes per nonzero) fits in half of L2: its steps are latency-bound
+        form = (B_ == 1 && 16.0 * (double)nnz_ <= kSoloMaxBytes) ? 2 : 0;
+    }
+    if (form == 2 && B_ != 1) form = 1;  // the single-LP form needs one LP
+    return set_form(form);
+}
+
+// Step form in use: 0 kernels per phase (graphs), 1 / 2 persistent.
+int MixedSolver::set_form(int form) {
+    if (form != 0 && (form == 1 ? grid_form1_ : grid_form2_) < 1) {
+        if (opts_.persistent > 0)
+            return fail(SIH_PDHG_ERR_UNSUPPORTED, "options.persistent: no cooperative launch of the step kernel here");
+        form = 0;
+    }
+    persistent_ = form;
+    pgrid_ = form == 1 ? grid_form1_ : (form == 2 ? grid_form2_ : 0);
     return SIH_PDHG_OK;
 }
 
@@ -1664,6 +1716,8 @@ int MixedSolver::choose_staging() {
     };
     SIHG_TRY(enable((const void*)k_step_dual_staged, stage_x_, stage_x_));
     SIHG_TRY(enable((const void*)k_step_kty_staged, stage_y_, stage_y_));
+    stage_x_rule_ = stage_x_;
+    stage_y_rule_ = stage_y_;
     if (opts_.verbose)
         std::fprintf(stderr, "sih_pdhg setup: staged gathers: %d entries of x, %d of y\n", stage_x_, stage_y_);
     return SIH_PDHG_OK;
@@ -1707,6 +1761,10 @@ int MixedSolver::reset_state() {
         S.W = 0.0;
         S.avg_w = 0.0;
         S.kkt_last = S.kkt_prev = 0.0;
+        S.tol_p = cfg_.tol_primal;
+        S.tol_d = cfg_.tol_dual;
+        S.tol_g = cfg_.tol_gap;
+        S.verify_rounds = 0;
     }
     SIHG_CUDA(cudaMemcpyAsync(state_.as<Inst>(), host_inst_.data(), sizeof(Inst) * B_, cudaMemcpyHostToDevice, s));
     SIHG_CUDA(cudaMemsetAsync(done_count_.as<void>(), 0, sizeof(unsigned), s));
@@ -1780,17 +1838,20 @@ int MixedSolver::run() {
         cudaError_t e = cudaEventCreateWithFlags(&ev[w], cudaEventDisableTiming);
         if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventCreate", __FILE__, __LINE__);
     }
-    // the evaluation that ends block k sees attempts = (k + 1) * eval_freq and
+    // the evaluation that ends block k sees attempts <= (k + 1) * eval_freq and
     // stops every instance at the iteration limit, so this many blocks suffice
     const long long max_blocks = std::max<long long>(1, (cfg_.max_iterations + eval_freq_ - 1) / eval_freq_);
+    long long blk = 0;
     timed_out_ = false;
-    if (rc == SIH_PDHG_OK) {
-        cudaEventRecord(ev_start_, s);
-        for (long long blk = 0; blk < max_blocks && rc == SIH_PDHG_OK; ++blk) {
-            const int slot = (int)(blk % kWindow);
-            if (blk >= kWindow) {
+    // Blocks of eval_freq steps and one evaluation until every instance
+    // stopped (a window of kWindow blocks in flight; the done count of the
+    // oldest is read back before the next is queued).
+    auto run_blocks = [&]() -> int {
+        for (long long k = 0; blk < max_blocks; ++blk, ++k) {
+            const int slot = (int)(k % kWindow);
+            if (k >= kWindow) {
                 cudaError_t e = cudaEventSynchronize(ev[slot]);
-                if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__); break; }
+                if (e != cudaSuccess) return cuda_fail(e, "cudaEventSynchronize", __FILE__, __LINE__);
                 if ((int)h_done[slot] >= B_) break;
                 if (opts_.time_limit_sec > 0 &&
                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() > opts_.time_limit_sec) {
@@ -1799,35 +1860,79 @@ int MixedSolver::run() {
                 }
             }
             if (persistent_) {
-                rc = launch_persistent(s, eval_freq_);
-                if (rc == SIH_PDHG_OK) rc = launch_eval(s);
+                SIHG_TRY(launch_persistent(s, eval_freq_));
+                SIHG_TRY(launch_eval(s));
             } else if (graph) {
                 cudaError_t e = cudaGraphLaunch(graphs_[0], s);
-                if (e != cudaSuccess) { rc = cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__); break; }
+                if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__);
                 launches_ += 3ull * eval_freq_ + 6ull;
             } else {
-                for (int k = 0; k < eval_freq_ && rc == SIH_PDHG_OK; ++k) rc = launch_step(s);
-                if (rc == SIH_PDHG_OK) rc = launch_eval(s);
+                for (int j = 0; j < eval_freq_; ++j) SIHG_TRY(launch_step(s));
+                SIHG_TRY(launch_eval(s));
             }
             cudaMemcpyAsync(&h_done[slot], done_count_.as<unsigned>(), sizeof(unsigned), cudaMemcpyDeviceToHost, s);
             cudaEventRecord(ev[slot], s);
         }
         cudaEventRecord(ev_stop_, s);
         cudaError_t e = cudaStreamSynchronize(s);
-        if (rc == SIH_PDHG_OK && e != cudaSuccess) rc = cuda_fail(e, "iteration loop", __FILE__, __LINE__);
+        if (e != cudaSuccess) return cuda_fail(e, "iteration loop", __FILE__, __LINE__);
+        if (persistent_) {
+            int status = 0;
+            SIHG_CUDA(cudaMemcpy(&status, bar_.as<unsigned long long>() + 1, sizeof(int), cudaMemcpyDeviceToHost));
+            if (status != 0)
+                return fail(SIH_PDHG_ERR_CUDA, "persistent step kernel: a grid barrier wait ran out (a block stopped "
+                                               "arriving); the solve was abandoned");
+        }
+        SIHG_CUDA(cudaMemcpy(host_inst_.data(), state_.as<Inst>(), sizeof(Inst) * B_, cudaMemcpyDeviceToHost));
+        return SIH_PDHG_OK;
+    };
+    if (rc == SIH_PDHG_OK) {
+        cudaEventRecord(ev_start_, s);
+        rc = run_blocks();
+    }
+    // The device stops an instance on relative KKT measures of its FP32 data
+    // and iterates (compensated, FP64 totals); the FP64 check of the returned
+    // point against the original FP64 problem can read a few percent higher
+    // near the tolerance.  An instance whose FP64 check fails goes on with its
+    // device tolerances scaled by 0.8 (at most kVerifyRounds times), so that a
+    // result reported optimal meets the tolerance in FP64.
+    constexpr int kVerifyRounds = 4;
+    for (int round = 0; rc == SIH_PDHG_OK && round < kVerifyRounds && !timed_out_ && blk < max_blocks; ++round) {
+        std::vector<int> redo;
+        std::vector<double> x, y;
+        for (int b = 0; b < B_ && rc == SIH_PDHG_OK; ++b) {
+            const Inst& S = host_inst_[b];
+            if (S.done != 1) continue;
+            rc = fetch(b, x, y);
+            if (rc != SIH_PDHG_OK) break;
+            const KktReport k = host_kkt(probs_[b]->src, x.data(), y.data(), nullptr, nullptr);
+            if (!(k.rel_primal <= cfg_.tol_primal && k.rel_dual <= cfg_.tol_dual && k.rel_gap <= cfg_.tol_gap))
+                redo.push_back(b);
+        }
+        if (rc != SIH_PDHG_OK || redo.empty()) break;
+        for (int b : redo) {
+            Inst& S = host_inst_[b];
+            S.done = 0;
+            S.tol_p *= 0.8;
+            S.tol_d *= 0.8;
+            S.tol_g *= 0.8;
+            S.verify_rounds += 1;
+            cudaError_t e = cudaMemcpyAsync(state_.as<Inst>() + b, &S, sizeof(Inst), cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync", __FILE__, __LINE__); break; }
+        }
+        if (rc != SIH_PDHG_OK) break;
+        unsigned ndone = 0;
+        for (int b = 0; b < B_; ++b) ndone += host_inst_[b].done != 0 ? 1u : 0u;
+        cudaError_t e = cudaMemcpyAsync(done_count_.as<unsigned>(), &ndone, sizeof(unsigned), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpyAsync", __FILE__, __LINE__); break; }
+        for (int w = 0; w < kWindow; ++w) h_done[w] = 0;
+        rc = launch_compact(s);  // the re-opened instances' tasks and chunks join the active lists
+        if (rc == SIH_PDHG_OK) rc = run_blocks();
     }
     for (int w = 0; w < kWindow; ++w)
         if (ev[w]) cudaEventDestroy(ev[w]);
     cudaFreeHost(h_done);
     if (rc != SIH_PDHG_OK) return rc;
-    if (persistent_) {
-        int status = 0;
-        SIHG_CUDA(cudaMemcpy(&status, bar_.as<unsigned long long>() + 1, sizeof(int), cudaMemcpyDeviceToHost));
-        if (status != 0)
-            return fail(SIH_PDHG_ERR_CUDA, "persistent step kernel: a grid barrier wait ran out (a block stopped "
-                                           "arriving); the solve was abandoned");
-    }
-    SIHG_CUDA(cudaMemcpy(host_inst_.data(), state_.as<Inst>(), sizeof(Inst) * B_, cudaMemcpyDeviceToHost));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev_start_, ev_stop_);
     loop_seconds_ = ms * 1e-3;
@@ -1938,49 +2043,172 @@ int MixedSolver::set_start(int b, const double* x, const double* y, double omega
     return SIH_PDHG_OK;
 }
 
-// SpMV task-size autotuner (options.autotune): times the two SpMV step
-// kernels for a ladder of task sizes on this batch and keeps the fastest.  The
+// Launch-shape autotuner (options.autotune): on this batch, times the two
+// step SpMVs over
+//   * the nonzeros per task (a ladder around the default),
+//   * the lanes per segment of the light tasks of each side (the length rule,
+//     or 1, 2, 4, 8 forced),
+//   * the staged gathers of a single LP (on / off per side),
+// one coordinate after the other, keeping the fastest, then (options.persistent
+// < 0) the step form: kernels per phase replayed as a graph, or the persistent
+// kernel, by the device time of a block of steps and an evaluation.  The
 // choice is cached per process for the shape (instances, rows, columns,
 // nonzeros), so repeated solves of one shape tune once.
-int MixedSolver::autotune() {
-    struct Key {
-        int b, m, n;
-        long long nnz;
-        bool operator<(const Key& o) const {
-            return std::tie(b, m, n, nnz) < std::tie(o.b, o.m, o.n, o.nnz);
+namespace {
+struct TuneKey {
+    int b, m, n;
+    long long nnz;
+    bool operator<(const TuneKey& o) const { return std::tie(b, m, n, nnz) < std::tie(o.b, o.m, o.n, o.nnz); }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, sih_pdhg_launch_shape> g_tune_cache;
+}  // namespace
+
+void MixedSolver::launch_shape(sih_pdhg_launch_shape* out) const {
+    out->task_nnz = task_nnz_;
+    out->row_lanes = lanes_r_;
+    out->col_lanes = lanes_c_;
+    out->staged_x = stage_x_;
+    out->staged_y = stage_y_;
+    out->persistent = persistent_;
+    out->grid = persistent_ ? pgrid_ : grid_;
+    out->tuned = tuned_;
+}
+
+// A cached shape; what the caller's options fix stays as they say.
+int MixedSolver::apply_shape(const sih_pdhg_launch_shape& sh) {
+    if (opts_.lanes_csr == 0) lanes_r_ = sh.row_lanes;
+    if (opts_.lanes_csc == 0) lanes_c_ = sh.col_lanes;
+    SIHG_TRY(build_schedules(opts_.tile_nnz > 0 ? task_nnz_ : sh.task_nnz));
+    stage_x_ = sh.staged_x ? stage_x_rule_ : 0;
+    stage_y_ = sh.staged_y ? stage_y_rule_ : 0;
+    return opts_.persistent < 0 ? set_form(sh.persistent) : SIH_PDHG_OK;
+}
+
+// Device seconds of one block of eval_freq steps and an evaluation in the
+// current step form, from the initial point (after one untimed block).
+int MixedSolver::time_block(double* seconds) {
+    eval_freq_ = opts_.eval_frequency > 0 ? opts_.eval_frequency : 64;
+    const bool graph = opts_.use_graph && !persistent_;
+    if (graph) SIHG_TRY(record_graph());
+    if (persistent_) SIHG_CUDA(cudaMemsetAsync(bar_.as<void>(), 0, 4 * sizeof(unsigned), stream_));
+    SIHG_TRY(reset_state());
+    cudaStream_t s = stream_;
+    auto block = [&]() -> int {
+        if (persistent_) {
+            SIHG_TRY(launch_persistent(s, eval_freq_));
+            return launch_eval(s);
         }
+        if (graph) {
+            SIHG_CUDA(cudaGraphLaunch(graphs_[0], s));
+            return SIH_PDHG_OK;
+        }
+        for (int j = 0; j < eval_freq_; ++j) SIHG_TRY(launch_step(s));
+        return launch_eval(s);
     };
-    static std::mutex mu;
-    static std::map<Key, int> cache;
-    const Key key{B_, M_, N_, nnz_};
+    SIHG_TRY(block());
+    constexpr int kBlocks = 2;
+    SIHG_CUDA(cudaEventRecord(ev_start_, s));
+    for (int k = 0; k < kBlocks; ++k) SIHG_TRY(block());
+    SIHG_CUDA(cudaEventRecord(ev_stop_, s));
+    SIHG_CUDA(cudaEventSynchronize(ev_stop_));
+    float ms = 0.f;
+    SIHG_CUDA(cudaEventElapsedTime(&ms, ev_start_, ev_stop_));
+    *seconds = ms * 1e-3 / kBlocks;
+    return SIH_PDHG_OK;
+}
+
+int MixedSolver::autotune() {
+    const TuneKey key{B_, M_, N_, nnz_};
     {
-        std::lock_guard<std::mutex> g(mu);
-        auto it = cache.find(key);
-        if (it != cache.end()) {
-            if (it->second != task_nnz_) SIHG_TRY(build_schedules(it->second));
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            SIHG_TRY(apply_shape(it->second));
+            tuned_ = 1;
             return SIH_PDHG_OK;
         }
     }
-    std::vector<int> ladder = {256, 384, 512, 768, 1024, 1536, 2048, task_nnz_};
-    std::sort(ladder.begin(), ladder.end());
-    ladder.erase(std::unique(ladder.begin(), ladder.end()), ladder.end());
-    int best = task_nnz_;
-    double best_t = INFINITY;
-    const int reps = nnz_ > 4000000 ? 5 : 20;
-    for (int t : ladder) {
-        if ((long long)t > std::max<long long>(nnz_, 256)) continue;
-        SIHG_TRY(build_schedules(t));
-        double sec[3];
+    const int reps = nnz_ > 64000000 ? 3 : (nnz_ > 4000000 ? 5 : 20);
+    double sec[3];
+    auto time_sides = [&](double& rows_s, double& cols_s) -> int {
         SIHG_TRY(time_kernels(reps, sec, nullptr));
-        const double spmv = sec[1] + sec[2];
-        if (spmv < best_t) {
-            best_t = spmv;
-            best = t;
+        rows_s = sec[1];
+        cols_s = sec[2];
+        return SIH_PDHG_OK;
+    };
+    double tr = 0, tc = 0;
+    // task size (lanes as configured)
+    int best_t = task_nnz_;
+    if (opts_.tile_nnz <= 0) {
+        std::vector<int> ladder = {384, 768, 1536, task_nnz_};
+        if (nnz_ <= 64000000) ladder.insert(ladder.end(), {256, 512, 1024, 2048});
+        std::sort(ladder.begin(), ladder.end());
+        ladder.erase(std::unique(ladder.begin(), ladder.end()), ladder.end());
+        double best = INFINITY;
+        for (int t : ladder) {
+            if ((long long)t > std::max<long long>(nnz_, 256)) continue;
+            SIHG_TRY(build_schedules(t));
+            SIHG_TRY(time_sides(tr, tc));
+            if (tr + tc < best) {
+                best = tr + tc;
+                best_t = t;
+            }
         }
     }
-    SIHG_TRY(build_schedules(best));
-    std::lock_guard<std::mutex> g(mu);
-    cache[key] = best;
+    // lanes per segment of each side's light tasks (0 = the length rule)
+    const std::vector<int> lane_ladder = {0, 1, 2, 4, 8};
+    for (int side = 0; side < 2; ++side) {
+        if ((side == 0 ? opts_.lanes_csr : opts_.lanes_csc) != 0) continue;  // fixed by the caller
+        int& lanes = side == 0 ? lanes_r_ : lanes_c_;
+        int best_l = lanes;
+        double best = INFINITY;
+        for (int L : lane_ladder) {
+            lanes = L;
+            SIHG_TRY(build_schedules(best_t));
+            SIHG_TRY(time_sides(tr, tc));
+            const double t = side == 0 ? tr : tc;
+            if (t < best) {
+                best = t;
+                best_l = L;
+            }
+        }
+        lanes = best_l;
+    }
+    SIHG_TRY(build_schedules(best_t));
+    // staged gathers (single LP): keep each side's only if it is faster
+    for (int side = 0; side < 2; ++side) {
+        int& st = side == 0 ? stage_x_ : stage_y_;
+        const int rule = side == 0 ? stage_x_rule_ : stage_y_rule_;
+        if (rule == 0) continue;
+        st = rule;
+        SIHG_TRY(time_sides(tr, tc));
+        const double on = side == 0 ? tr : tc;
+        st = 0;
+        SIHG_TRY(time_sides(tr, tc));
+        const double off = side == 0 ? tr : tc;
+        st = on <= off ? rule : 0;
+    }
+    // step form: graph of kernels per phase, or the persistent kernel
+    if (opts_.persistent < 0) {
+        const int alt = B_ == 1 ? 2 : 1;
+        if ((alt == 1 ? grid_form1_ : grid_form2_) > 0) {
+            double t0 = 0, t1 = 0;
+            SIHG_TRY(set_form(0));
+            SIHG_TRY(time_block(&t0));
+            SIHG_TRY(set_form(alt));
+            SIHG_TRY(time_block(&t1));
+            SIHG_TRY(set_form(t1 < t0 ? alt : 0));
+        }
+    }
+    tuned_ = 1;
+    sih_pdhg_launch_shape sh{};
+    launch_shape(&sh);
+    if (opts_.verbose)
+        std::fprintf(stderr, "sih_pdhg autotune: task_nnz %d, lanes rows %d cols %d, staged %d/%d, form %d\n",
+                     sh.task_nnz, sh.row_lanes, sh.col_lanes, sh.staged_x, sh.staged_y, sh.persistent);
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune_cache[key] = sh;
     return SIH_PDHG_OK;
 }
 

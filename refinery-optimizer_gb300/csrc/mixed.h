@@ -58,6 +58,8 @@ struct Inst {
     double kmax, b2, c2;
     double omega_start;  // > 0: initial primal weight of a warm start
     double pow06, pow03; // (attempts + 2)^-0.6 and ^-0.3 of the current attempt
+    int verify_rounds;   // times the FP64 check of a converged point sent the instance on
+    int pad_;
 };
 
 struct Side {
@@ -135,6 +137,9 @@ struct Vecs {
     // step-weighted running averages, accumulated in float-float (hi, lo);
     // x_avg / y_avg above are their FP32 copies, refreshed before every evaluation
     float2 *x_acc, *y_acc;
+    // (k^-0.6, k^-0.3) of the step-size schedule for k < pow_n
+    const double2* pow_tab;
+    int pow_n;
 };
 
 class MixedSolver {
@@ -163,6 +168,8 @@ class MixedSolver {
     int set_start(int b, const double* x, const double* y, double omega);
     int task_nnz() const { return task_nnz_; }
     bool persistent() const { return persistent_ != 0; }
+    // The launch shape in use (autotuner's choice or the rules).
+    void launch_shape(sih_pdhg_launch_shape* out) const;
     long long nnz() const { return nnz_; }
     int rows() const { return M_; }
     int cols() const { return N_; }
@@ -177,6 +184,9 @@ class MixedSolver {
     int launch_step_spmvs(cudaStream_t s, int which);
     int launch_persistent(cudaStream_t s, int nsteps);
     int setup_persistent();
+    int set_form(int form);
+    int apply_shape(const sih_pdhg_launch_shape& sh);
+    int time_block(double* seconds);
 
     std::vector<const HostProblem*> probs_;
     sih_pdhg_config cfg_{};
@@ -197,7 +207,7 @@ class MixedSolver {
     std::vector<int> col_perm_, row_perm_;  // device order -> instance-local original index
     std::vector<int> h_csr_ptr_, h_csc_ptr_;  // segment pointers (device order), for schedule rebuilds
     DevMem csr_ptr_, csc_ptr_, csr_pairs_, csc_pairs_;
-    DevMem colvec_, rowvec_, state_, done_count_, accvec_;
+    DevMem colvec_, rowvec_, state_, done_count_, accvec_, pow_tab_;
     TaskLayout layout_;
     Side rows_{}, cols_{};
     Chunks chunks_all_{};
@@ -208,8 +218,11 @@ class MixedSolver {
     // persistent step kernel (options.persistent): its grid (every block
     // resident) and the grid barrier's words {arrive, gen, status}
     // (1 = the task-engine form, 2 = the single-LP form with per-block partials)
-    int persistent_ = 0, pgrid_ = 0;
+    int persistent_ = 0, pgrid_ = 0, grid_form1_ = 0, grid_form2_ = 0;
     DevMem bar_, part_;
+    // lanes per segment of the light tasks (0 = length rule), staged prefixes
+    // the rule chose (the tuner may switch them off), tuned flag
+    int lanes_r_ = 0, lanes_c_ = 0, stage_x_rule_ = 0, stage_y_rule_ = 0, tuned_ = 0;
     Vecs V_{};
     std::vector<Inst> host_inst_;
     std::vector<std::vector<float>> start_x_, start_y_;  // warm starts (device order, unscaled)

@@ -16,8 +16,9 @@
 //     in in_solve_log instead of running the CPU simplex (the engine has no CPU
 //     fallback);
 //   * solve_hybrid keeps the reference's flow: PDHG, then a basis guessed from
-//     the PDHG point, then the FP64 simplex warm start, then a cold FP64 solve
-//     if the warm start does not reach optimality.
+//     the PDHG point (scored and selected on the GPU by sih_pdhg_basis_guess),
+//     then the FP64 simplex warm start, then a cold FP64 solve if the warm
+//     start does not reach optimality.
 #include <sih/gpu/gpu_solver.hpp>
 #include <sih/simplex/simplex_solver.hpp>
 
@@ -128,35 +129,20 @@ model::Solution GpuSolver::solve_hybrid(const model::Problem& problem, const Gpu
     polish.strategy.enable_scaling = false;
     polish.log_to_console = false;
     if (pd.status == model::SolutionStatus::NumericalFailure) return pd;
-    // Basis guess: rank columns (value x) and rows (activity A x) by their
-    // distance to the nearest finite bound; the m most interior become basic,
-    // the rest sit at their nearer bound.
-    struct Cand {
-        int64_t id;
-        double dist;
-        bool at_lower;
-    };
-    std::vector<Cand> cands;
-    cands.reserve(n + m);
-    auto push = [&](int64_t id, double v, double lo, double hi) {
-        const double dl = (lo > -1e15) ? std::max(0.0, v - lo) : 1e30;
-        const double du = (hi < 1e15) ? std::max(0.0, hi - v) : 1e30;
-        cands.push_back(Cand{id, std::min(dl, du), dl <= du});
-    };
-    for (int64_t j = 0; j < n; ++j) push(j, pd.x[j], problem.col_lower()[j], problem.col_upper()[j]);
-    for (int64_t i = 0; i < m; ++i) push(n + i, pd.slack[i], problem.row_lower()[i], problem.row_upper()[i]);
-    std::stable_sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& b) { return a.dist > b.dist; });
-    std::vector<model::BasisStatus> cb(n, model::BasisStatus::AtLower), rb(m, model::BasisStatus::AtLower);
-    for (size_t k = 0; k < cands.size(); ++k) {
-        const Cand& c = cands[k];
-        const model::BasisStatus st = (int64_t)k < m ? model::BasisStatus::Basic
-                                                     : (c.at_lower ? model::BasisStatus::AtLower
-                                                                   : model::BasisStatus::AtUpper);
-        if (c.id < n)
-            cb[c.id] = st;
-        else
-            rb[c.id - n] = st;
+    // Basis guess on the GPU (sih_pdhg_basis_guess): columns (value x) and rows
+    // (activity A x, the slack the engine returned) ranked by their distance to
+    // the nearest finite bound; the m most interior become basic, the rest sit
+    // at their nearer bound (the reference's scoring, gpu_solver.cpp:332-395).
+    const sih_pdhg_problem q = to_c_problem(problem);
+    std::vector<int8_t> cs(n), rs(m);
+    if (sih_pdhg_basis_guess(&q, pd.x.data(), pd.slack.data(), cs.data(), rs.data()) != SIH_PDHG_OK) {
+        pd.status = model::SolutionStatus::NumericalFailure;
+        pd.in_solve_log = sih_pdhg_last_error();
+        return pd;
     }
+    std::vector<model::BasisStatus> cb(n), rb(m);
+    for (int64_t j = 0; j < n; ++j) cb[j] = static_cast<model::BasisStatus>(cs[j]);
+    for (int64_t i = 0; i < m; ++i) rb[i] = static_cast<model::BasisStatus>(rs[i]);
     model::Solution sol = simplex::SimplexSolver::solve_from_basis(problem, cb, rb, polish);
     if (!sol.is_optimal()) sol = simplex::SimplexSolver::solve(problem, polish);
     sol.time_wall_sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -133,6 +133,14 @@ class PdhgHandle:
         _lib.check(self._lib.sih_pdhg_get_task_nnz(self._h, C.byref(v)))
         return v.value
 
+    def launch_shape(self) -> dict:
+        """Launch shape of the step kernels (sih_pdhg_get_launch_shape): task size,
+        lanes per segment of each side, staged gathers, step form, grid, and
+        whether the autotuner chose it."""
+        sh = _lib.CLaunchShape()
+        _lib.check(self._lib.sih_pdhg_get_launch_shape(self._h, C.byref(sh)))
+        return {f: getattr(sh, f) for f, _ in _lib.CLaunchShape._fields_}
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.sih_pdhg_destroy(self._h)
@@ -195,6 +203,24 @@ def adjoint_batch(problems, xs, row_duals, grad_xs, tolerance: float = 1e-6, max
     del keep
     return out, [{k: getattr(infos[i], k) for k, _ in _lib.CAdjointInfo._fields_ if k != "reserved"}
                  for i in range(B)]
+
+
+def basis_guess(problem: Problem, x, row_activity):
+    """Basis guess of the hybrid polish on the GPU (sih_pdhg_basis_guess; the
+    scoring of GpuSolver::solve_hybrid, core/src/gpu/gpu_solver.cpp:332-395):
+    the m columns / rows farthest from their nearer finite bound are Basic (0),
+    the others AtLower (1) or AtUpper (2).  Returns (col_status, row_status) as
+    int8 arrays, values of sih::model::BasisStatus."""
+    lib = _lib.load()
+    cp, keep = _lib.c_problem(problem)
+    xa = np.ascontiguousarray(x, dtype=np.float64)
+    ax = np.ascontiguousarray(row_activity, dtype=np.float64)
+    if xa.shape != (problem.num_cols(),) or ax.shape != (problem.num_rows(),):
+        raise SihPdhgError(1, "x / row_activity do not match the problem's shape")
+    cs = np.empty(problem.num_cols(), dtype=np.int8)
+    rs = np.empty(problem.num_rows(), dtype=np.int8)
+    _lib.check(lib.sih_pdhg_basis_guess(C.byref(cp), xa.ctypes.data, ax.ctypes.data, cs.ctypes.data, rs.ctypes.data))
+    return cs, rs
 
 
 def polish_batch(problems, xs, row_duals, tolerance: float = 1e-6, max_iterations: int = 0):

@@ -51,6 +51,12 @@ class COptions(C.Structure):
                 ("persistent", C.c_int32)]
 
 
+class CLaunchShape(C.Structure):
+    _fields_ = [("task_nnz", C.c_int32), ("row_lanes", C.c_int32), ("col_lanes", C.c_int32),
+                ("staged_x", C.c_int32), ("staged_y", C.c_int32), ("persistent", C.c_int32), ("grid", C.c_int32),
+                ("tuned", C.c_int32)]
+
+
 class CAdjointOptions(C.Structure):
     _fields_ = [("struct_size", C.c_int32), ("reserved", C.c_int32), ("tolerance", C.c_double),
                 ("max_iterations", C.c_int64)]
@@ -116,6 +122,8 @@ def load() -> C.CDLL:
     lib.sih_pdhg_time_kernels.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.sih_pdhg_set_start.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double]
     lib.sih_pdhg_get_task_nnz.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    lib.sih_pdhg_basis_guess.argtypes = [C.POINTER(CProblem), vp, vp, vp, vp]
+    lib.sih_pdhg_get_launch_shape.argtypes = [C.c_void_p, C.POINTER(CLaunchShape)]
     lib.sih_pdhg_check_grid_barrier.argtypes = [i32, i32, i32, C.c_double, C.POINTER(C.c_int32),
                                                 C.POINTER(C.c_int32)]
     lib.sih_pdhg_adjoint_options_default.argtypes = [C.c_void_p]

@@ -15,7 +15,10 @@ column, where no basis read off a 1e-6 point was optimal): the instance returns
 its PDHG point instead, which satisfies the LP to the solve's tolerance, a
 ``LPLayerWarning`` names the instances, and their gradients are those of the
 basis that was read, an approximation.
-Backward: the adjoint kernel (sih_pdhg_adjoint_batch): the active pattern of
+Optimal values (return_objective=True): v* = c^T x* with gradients from the
+duals by the envelope theorem (objective_gradients), exact at the returned
+point and independent of the basis.
+Backward of x*: the adjoint kernel (sih_pdhg_adjoint_batch): the active pattern of
 the PDHG fixed point read off (x*, y*) as a basis, and B^T lambda = dL/dx_F
 solved on the GPU by CGLS with the engine's SpMVs.  Gradients flow to the row
 bounds and column bounds; the objective's implicit gradient is zero (an LP
@@ -63,6 +66,33 @@ def choose_outputs(sols, xs, ys, infos, certify_tol: float):
     return x_out, y_out, bad
 
 
+def objective_gradients(problem: Problem, x, y_pdhg) -> dict:
+    """Gradient of the optimal value v = c^T x* of a minimisation LP with respect
+    to its data, from a primal-dual optimal pair (the envelope theorem, i.e. LP
+    sensitivity analysis; no linear system): dv/dc = x*, dv/d row bound = the
+    simplex dual y = -y_pdhg (to row_lower where y > 0 or the row is an
+    equality, to row_upper where y < 0), dv/d column bound = the reduced cost
+    lambda = c - A^T y (to col_lower where lambda > 0, to col_upper where
+    lambda < 0, finite bounds only).  Needs no basis, so it is as accurate as
+    the PDHG point itself on LPs whose basis the polish cannot identify."""
+    A = problem.A
+    m, n = problem.num_rows(), problem.num_cols()
+    y = -np.asarray(y_pdhg, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64)
+    cp, ri, cv = A.csc_col_ptr(), A.csc_row_ind(), A.csc_values()
+    aty = np.zeros(n)
+    cols = np.repeat(np.arange(n), np.diff(cp))
+    np.add.at(aty, cols, cv * y[ri])
+    lam = problem.c - aty
+    eq = problem.row_lower == problem.row_upper
+    g_rl = np.where(eq, y, np.maximum(y, 0.0))
+    g_ru = np.where(eq, 0.0, np.minimum(y, 0.0))
+    g_l = np.where(np.isfinite(problem.col_lower), np.maximum(lam, 0.0), 0.0)
+    g_u = np.where(np.isfinite(problem.col_upper), np.minimum(lam, 0.0), 0.0)
+    return {"c": x.copy(), "row_lower": g_rl, "row_upper": g_ru, "col_lower": g_l, "col_upper": g_u,
+            "objective": float(problem.c @ x)}
+
+
 def _problems(mats: List[SparseMatrix], c, rl, ru, l, u) -> List[Problem]:
     out = []
     for i, A in enumerate(mats):
@@ -73,7 +103,8 @@ def _problems(mats: List[SparseMatrix], c, rl, ru, l, u) -> List[Problem]:
 if torch is not None:
 
     class LPFunction(torch.autograd.Function):
-        """autograd.Function (c, row_lower, row_upper, col_lower, col_upper) -> x*."""
+        """autograd.Function (c, row_lower, row_upper, col_lower, col_upper) -> (x*, v*),
+        v* = c^T x* the optimal value of each instance."""
 
         @staticmethod
         def forward(ctx, c, row_lower, row_upper, col_lower, col_upper, mats, config, adjoint_tol, certify_tol):
@@ -99,24 +130,42 @@ if torch is not None:
             ctx.polish_info = infos
             ctx.adjoint_tol = adjoint_tol
             ctx.device = c.device
-            return torch.from_numpy(np.stack(xs)).to(c.device)
+            ctx.obj_grads = [objective_gradients(p, x, y) for p, x, y in zip(probs, xs, ys)]
+            x_t = torch.from_numpy(np.stack(xs)).to(c.device)
+            v_t = torch.tensor([d["objective"] for d in ctx.obj_grads], dtype=torch.float64, device=c.device)
+            return x_t, v_t
 
         @staticmethod
-        def backward(ctx, grad_x):
-            g = grad_x.detach().to("cpu", torch.float64).numpy()
-            grads, infos = adjoint_batch(ctx.probs, ctx.xs, ctx.ys, list(g), tolerance=ctx.adjoint_tol)
-            ctx.adjoint_info = infos
-            stack = lambda k: torch.from_numpy(np.stack([d[k] for d in grads])).to(ctx.device)
-            return (stack("c"), stack("row_lower"), stack("row_upper"), stack("col_lower"), stack("col_upper"),
+        def backward(ctx, grad_x, grad_v):
+            keys = ("c", "row_lower", "row_upper", "col_lower", "col_upper")
+            out = {k: np.stack([np.zeros_like(d[k]) for d in ctx.obj_grads]) for k in keys}
+            if grad_x is not None:
+                g = grad_x.detach().to("cpu", torch.float64).numpy()
+                if np.any(g):  # the solution map: adjoint system on the identified basis
+                    grads, infos = adjoint_batch(ctx.probs, ctx.xs, ctx.ys, list(g), tolerance=ctx.adjoint_tol)
+                    ctx.adjoint_info = infos
+                    for k in keys:
+                        out[k] += np.stack([d[k] for d in grads])
+            if grad_v is not None:  # the optimal value: envelope theorem, exact at the returned point
+                gv = grad_v.detach().to("cpu", torch.float64).numpy()
+                for k in keys:
+                    out[k] += gv[:, None] * np.stack([d[k] for d in ctx.obj_grads])
+            to_t = lambda k: torch.from_numpy(out[k]).to(ctx.device)
+            return (to_t("c"), to_t("row_lower"), to_t("row_upper"), to_t("col_lower"), to_t("col_upper"),
                     None, None, None, None)
 
     def lp_layer(mats: List[SparseMatrix], c, row_lower, row_upper, col_lower, col_upper,
-                 config: Optional[GpuPdhgConfig] = None, adjoint_tol: float = 1e-6, certify_tol: float = 1e-6):
+                 config: Optional[GpuPdhgConfig] = None, adjoint_tol: float = 1e-6, certify_tol: float = 1e-6,
+                 return_objective: bool = False):
         """x* of each LP of the batch (a (batch, n) float64 tensor), differentiable
         with respect to the bounds (and c, with a zero implicit part).  Instances
         whose polished vertex is not certified within ``certify_tol`` return their
-        PDHG point (with an LPLayerWarning)."""
+        PDHG point (with an LPLayerWarning).  With return_objective, also the
+        optimal values v* = c^T x* (a (batch,) tensor) whose gradients come from
+        the duals (objective_gradients): write an objective term of a loss as
+        v* rather than c^T x* to differentiate it without the basis."""
         cfg = config if config is not None else GpuPdhgConfig(max_iterations=1_000_000, tol_primal=1e-6,
                                                                tol_dual=1e-6, tol_gap=1e-6)
-        return LPFunction.apply(c, row_lower, row_upper, col_lower, col_upper, list(mats), cfg, adjoint_tol,
+        x, v = LPFunction.apply(c, row_lower, row_upper, col_lower, col_upper, list(mats), cfg, adjoint_tol,
                                 certify_tol)
+        return (x, v) if return_objective else x

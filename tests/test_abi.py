@@ -47,7 +47,8 @@ def test_struct_layouts_match_header(tmp_path):
 
     src = tmp_path / "sizes.c"
     fields = {"sih_pdhg_config": GpuPdhgConfig, "sih_pdhg_options": _lib.COptions,
-              "sih_pdhg_result": _lib.CResult, "sih_pdhg_problem": _lib.CProblem}
+              "sih_pdhg_result": _lib.CResult, "sih_pdhg_problem": _lib.CProblem,
+              "sih_pdhg_launch_shape": _lib.CLaunchShape}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sih_pdhg.h"', "int main(void){"]
     for sname, cls in fields.items():
         lines.append(f'printf("{sname} %zu\\n", sizeof({sname}));')

@@ -51,9 +51,12 @@ def test_batch_matches_single_solves(sih):
              "rand_100x250_k6_s0"]
     probs = [golden_case(n)[0] for n in names]
     entries = [golden_case(n)[1] for n in names]
-    batch = sih.solve_batch(probs, cfg(sih))
+    # one launch shape for batch and single solves (no autotuning, kernels per
+    # phase): each instance then computes what it computes alone
+    same = dict(autotune=0, persistent=0)
+    batch = sih.solve_batch(probs, cfg(sih), **same)
     for p, e, r in zip(probs, entries, batch):
-        single = sih.solve_gpu_mixed(p, cfg(sih))
+        single = sih.solve_gpu_mixed(p, cfg(sih), **same)
         assert r.is_optimal()
         assert r.rel_primal <= 2e-4 and r.rel_gap <= 2e-4
         assert abs(r.simplex_iterations - single.simplex_iterations) <= 2 * 64

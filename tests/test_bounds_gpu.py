@@ -66,9 +66,12 @@ def test_exact_plain_path_is_bit_identical_to_the_oracle(sih, oracle_lib, seed):
 def test_batch_with_every_bound_kind(sih):
     probs = [_lp(s) for s in SEEDS] + [golden_case("rand_200x500_k8_s0")[0]]
     tol = 1e-4
-    batch = sih.solve_batch(probs, _cfg(sih, tol))
+    # one launch shape for batch and single solves (no autotuning, kernels per
+    # phase): each instance then computes what it computes alone
+    same = dict(autotune=0, persistent=0)
+    batch = sih.solve_batch(probs, _cfg(sih, tol), **same)
     for p, r in zip(probs, batch):
-        single = sih.solve_gpu_mixed(p, _cfg(sih, tol))
+        single = sih.solve_gpu_mixed(p, _cfg(sih, tol), **same)
         assert r.is_optimal()
         assert r.rel_primal <= 2 * tol and r.rel_dual <= 2 * tol and r.rel_gap <= 2 * tol
         assert abs(r.simplex_iterations - single.simplex_iterations) <= 2 * 64

@@ -1,7 +1,7 @@
 """Multi-process paths of bench.py on CPU (gloo, world size 2): the max-over-
-ranks timing reduction, the per-rank workload seeds of the replica layout,
-and the reference arm's launch contract (rank 0 prints one JSON line, the
-other ranks exit 0 without output)."""
+ranks timing reduction, the instance partition of a batch with its host
+gather, and the reference arm's launch contract (rank 0 prints one JSON line,
+the other ranks exit 0 without output)."""
 import json
 import os
 import socket
@@ -29,13 +29,23 @@ def _worker(rank, world, port, out):
 
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
     try:
+        batch = [f"scenario{i}" for i in range(7)]
+        mine, idx = bench.shard(batch, rank, world)
+        # each rank "solves" its shard: one summary row per instance it holds
+        rows = [{"index": i, "iterations": 100 * i + rank} for i in idx]
+        gathered = bench.gather_instances(rows, world)
         out[rank] = (bench.reduce_max(float(rank + 1) * 0.5, world, "cpu"),
-                     bench.workload_seed("refinery-512", rank), bench.workload_seed("zipf-500kx1m", rank))
+                     bench.workload_seed("refinery-512", rank), bench.workload_seed("zipf-500kx1m", rank),
+                     mine, [r["index"] for r in gathered], [r["iterations"] for r in gathered],
+                     bench.reduce_sum([1.0, float(rank)], world, "cpu"))
     finally:
         dist.destroy_process_group()
 
 
-def test_reduce_max_and_seeds_world_size_2():
+def test_partition_gather_and_timing_world_size_2():
+    """The batch partition: every rank builds the same batch (seed 0), takes
+    instances rank, rank + 2, ...; the host gather gives every rank all rows in
+    batch order; times reduce by max, byte counts by sum."""
     import torch.multiprocessing as mp
 
     port = _free_port()
@@ -43,8 +53,13 @@ def test_reduce_max_and_seeds_world_size_2():
     out = mgr.dict()
     mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
     assert out[0][0] == out[1][0] == 1.0
-    assert {out[0][1], out[1][1]} == {0, 1}  # own batch per rank
-    assert out[0][2] == out[1][2] == 0  # the same single LP on every rank
+    assert out[0][1] == out[1][1] == 0 and out[0][2] == out[1][2] == 0  # one workload, built alike
+    assert out[0][3] == ["scenario0", "scenario2", "scenario4", "scenario6"]
+    assert out[1][3] == ["scenario1", "scenario3", "scenario5"]
+    for r in (0, 1):
+        assert out[r][4] == list(range(7))
+        assert out[r][5] == [100 * i + (i % 2) for i in range(7)]
+        assert out[r][6] == [2.0, 1.0]
 
 
 def test_reference_arm_under_torchrun_world_size_2():

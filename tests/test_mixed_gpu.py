@@ -135,9 +135,10 @@ def test_staged_gathers_are_bit_identical(sih):
 
     prob = zipf_lp(20_000, 40_000, 480_000, seed=3)
     cfg = sih.GpuPdhgConfig(max_iterations=3000, tol_primal=1e-4, tol_dual=1e-4, tol_gap=1e-4)
-    off = sih.solve_gpu_mixed(prob, cfg, staged_kib=-1)
+    # staging belongs to the kernel-per-phase step form (persistent = 0)
+    off = sih.solve_gpu_mixed(prob, cfg, staged_kib=-1, persistent=0)
     for kib in (16, 0):
-        on = sih.solve_gpu_mixed(prob, cfg, staged_kib=kib)
+        on = sih.solve_gpu_mixed(prob, cfg, staged_kib=kib, persistent=0)
         assert on.status == off.status
         assert on.simplex_iterations == off.simplex_iterations
         np.testing.assert_array_equal(on.x, off.x)

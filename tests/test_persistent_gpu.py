@@ -29,7 +29,7 @@ def cfg(sih, tol=1e-4):
 @pytest.mark.parametrize("name", ["rand_200x500_k8_s0", "rand_2000x5000_k8_s0", "toy04_lp_equality_ranges"])
 def test_persistent_equals_graph_path(sih, name):
     prob, _, _ = golden_case(name)
-    a = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6))
+    a = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6), persistent=0)
     b = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6), persistent=1)
     assert a.is_optimal() and b.is_optimal()
     assert a.simplex_iterations == b.simplex_iterations and a.restarts == b.restarts
@@ -43,7 +43,7 @@ def test_persistent_batch_equals_graph_batch(sih):
     from sih_pdhg.generators import mixed_bounds_lp, refinery_lp, small_random_lp
 
     probs = [small_random_lp(300, 700, 6, 3), mixed_bounds_lp(seed=1), refinery_lp(24, 1), small_random_lp(50, 120, 4, 2)]
-    a = sih.solve_batch(probs, cfg(sih))
+    a = sih.solve_batch(probs, cfg(sih), persistent=0)
     b = sih.solve_batch(probs, cfg(sih), persistent=1)
     iters = {r.simplex_iterations for r in a}
     assert len(iters) > 1, "instances should stop at different evaluations"
@@ -95,7 +95,7 @@ def test_single_lp_persistent_form_solves_like_the_graph_path(sih, name):
     other roundings than the ticket chain, so the trajectory may differ in the
     last bits: same status, tolerance reached, the same optimum."""
     prob, entry, _ = golden_case(name)
-    a = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6))
+    a = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6), persistent=0)
     b = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6), persistent=2)
     assert a.is_optimal() and b.is_optimal()
     assert max(b.rel_primal, b.rel_dual, b.rel_gap) <= 2e-6
@@ -116,3 +116,25 @@ def test_single_lp_persistent_form_is_deterministic(sih):
     assert a.is_optimal() and a.simplex_iterations == b.simplex_iterations
     np.testing.assert_array_equal(a.x, b.x)
     np.testing.assert_array_equal(a.row_duals, b.row_duals)
+
+
+def test_automatic_form_and_launch_shape(sih):
+    """persistent = -1 (default): the single-LP form for a small LP, kernels per
+    phase for a large one; a batch is autotuned (autotune = -1) and reports the
+    shape it chose; a second handle of the same shape reuses it."""
+    from sih_pdhg.generators import small_random_lp
+
+    small = small_random_lp(200, 500, 8, 0)
+    with sih.PdhgHandle(small, cfg(sih), algorithm=sih.ALGO_MIXED) as h:
+        sh = h.launch_shape()
+        assert sh["persistent"] == 2 and sh["tuned"] == 0
+    batch = [small_random_lp(300, 700, 6, s) for s in range(3)]
+    with sih.PdhgHandle(batch, cfg(sih), algorithm=sih.ALGO_MIXED) as h:
+        sh = h.launch_shape()
+        h.run()
+        res = [h.result(b) for b in range(3)]
+    assert sh["tuned"] == 1 and sh["persistent"] in (0, 1)
+    assert sh["row_lanes"] in (0, 1, 2, 4, 8) and sh["col_lanes"] in (0, 1, 2, 4, 8)
+    assert all(r.is_optimal() for r in res)
+    with sih.PdhgHandle(batch, cfg(sih), algorithm=sih.ALGO_MIXED) as h:
+        assert h.launch_shape() == sh
