@@ -1841,13 +1841,13 @@ int MixedSolver::run() {
     // the evaluation that ends block k sees attempts <= (k + 1) * eval_freq and
     // stops every instance at the iteration limit, so this many blocks suffice
     const long long max_blocks = std::max<long long>(1, (cfg_.max_iterations + eval_freq_ - 1) / eval_freq_);
-    long long blk = 0;
+    long long blk = 0, blk_end = max_blocks;
     timed_out_ = false;
     // Blocks of eval_freq steps and one evaluation until every instance
     // stopped (a window of kWindow blocks in flight; the done count of the
     // oldest is read back before the next is queued).
     auto run_blocks = [&]() -> int {
-        for (long long k = 0; blk < max_blocks; ++blk, ++k) {
+        for (long long k = 0; blk < blk_end; ++blk, ++k) {
             const int slot = (int)(k % kWindow);
             if (k >= kWindow) {
                 cudaError_t e = cudaEventSynchronize(ev[slot]);
@@ -1897,7 +1897,7 @@ int MixedSolver::run() {
     // device tolerances scaled by 0.8 (at most kVerifyRounds times), so that a
     // result reported optimal meets the tolerance in FP64.
     constexpr int kVerifyRounds = 4;
-    for (int round = 0; rc == SIH_PDHG_OK && round < kVerifyRounds && !timed_out_ && blk < max_blocks; ++round) {
+    for (int round = 0; rc == SIH_PDHG_OK && round <= kVerifyRounds && !timed_out_; ++round) {
         std::vector<int> redo;
         std::vector<double> x, y;
         for (int b = 0; b < B_ && rc == SIH_PDHG_OK; ++b) {
@@ -1910,6 +1910,15 @@ int MixedSolver::run() {
                 redo.push_back(b);
         }
         if (rc != SIH_PDHG_OK || redo.empty()) break;
+        if (round == kVerifyRounds) {  // still above the tolerance in FP64: not reported as optimal
+            for (int b : redo) host_inst_[b].done = 4;
+            break;
+        }
+        // blocks enough for the re-opened instance with the fewest attempts to
+        // reach the iteration limit (the evaluation stops each at its limit)
+        long long min_attempts = cfg_.max_iterations;
+        for (int b : redo) min_attempts = std::min(min_attempts, host_inst_[b].attempts);
+        blk_end = blk + std::max<long long>(1, (cfg_.max_iterations - min_attempts + eval_freq_ - 1) / eval_freq_);
         for (int b : redo) {
             Inst& S = host_inst_[b];
             S.done = 0;
@@ -2243,6 +2252,9 @@ void MixedSolver::fill_result(int b, sih_pdhg_result* r) const {
         case 1: r->status = SIH_STATUS_OPTIMAL; break;
         case 2: r->status = SIH_STATUS_ITERATION_LIMIT; break;
         case 3: r->status = SIH_STATUS_NUMERICAL_FAILURE; break;
+        // the device test passed, the FP64 check of the point failed after the
+        // verification rounds: the FP32 data cannot get this instance closer
+        case 4: r->status = SIH_STATUS_NUMERICAL_FAILURE; break;
         default: r->status = timed_out_ ? SIH_STATUS_TIME_LIMIT : SIH_STATUS_ITERATION_LIMIT; break;
     }
     r->iterations = S.attempts;

@@ -34,7 +34,8 @@ constexpr int kTaskSegs = 1024;  // max segments per light task
 // Per-instance device state (reduction totals and controller scalars in FP64).
 struct Inst {
     // control
-    int done;          // 0 running, 1 converged, 2 iteration limit, 3 numerical failure
+    int done;          // 0 running, 1 converged, 2 iteration limit, 3 numerical failure,
+                       // 4 converged on the device but above the tolerance in the FP64 check
     int cur;           // buffer holding the current iterate (0 / 1)
     int avg_pending;   // the averages still need the last accepted iterate (weight avg_w)
     int restart_flag;  // set by an evaluation: 0 none, 1 restart at current, 2 restart at average

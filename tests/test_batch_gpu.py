@@ -98,3 +98,4 @@ def test_result_before_run_is_an_error(sih):
             h.result(0)
         with pytest.raises(sih.SihPdhgError):
             h.result(3)
+
