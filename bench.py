@@ -69,11 +69,13 @@ PLAIN_CAP = {
 }
 
 # DRAM bytes per launch of the dominant kernels, read from one ncu capture of
-# the same kernel on the same workload (dram__bytes_read.sum + write.sum of one
-# launch in `python bench.py --profile-solve 64`; summaries in profiles/).
+# the same kernels on the same workload (dram__bytes_read.sum + write.sum, mean
+# of the first two launches of each in `ncu --metrics dram__bytes_read.sum,
+# dram__bytes_write.sum,gpu__time_duration.sum --clock-control none -k
+# regex:k_step_ -c 6 python bench.py --profile-solve 64`; summaries in profiles/).
 NCU_TRAFFIC_PER_LAUNCH = {
-    ("zipf-500kx1m", "k_step_kty"): 119.71e6,
-    ("zipf-500kx1m", "k_step_dual"): 115.53e6,
+    ("zipf-500kx1m", "k_step_kty"): 117.22e6,
+    ("zipf-500kx1m", "k_step_dual"): 112.58e6,
 }
 
 

@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(kThreads, 4)
 // barrier is needed; block 0 writes the state back when the launch ends.
 // Deterministic; the sums are grouped differently from the task engine's, so
 // the iterates agree with the other forms to rounding, not bit for bit.
-constexpr int kSoloThreads = 768;
+constexpr int kSoloThreads = 640;  // 20 warps per SM at 96 registers (measured best of 512 / 640 / 768 / 1024)
 // Automatic step form: the single-LP form when the matrix (both sides) takes
 // at most this many bytes, half of the 129 MB L2 (measured per step: 80k
 // nonzeros 30.9 -> 20.8 us, 1.1M nonzeros 46.1 -> 38.8 us).
@@ -474,8 +474,78 @@ __device__ __forceinline__ void solo_side(const Side& side, const Inst& S, Epi& 
     epi.values(q);
 }
 
+// The single-LP form needs two grid barriers per step, not three: the
+// primal step x' = clip(x - tau (c + K^T y), l, u) is not written by an
+// elementwise phase before K x' gathers it, but computed by the gathering lane
+// from a packed record per column, pack[j] = {x_j, c_j + (K^T y)_j, l_j, u_j}
+// (one 16-byte load, the same L2 sector count as a float gather), with the
+// same operations as the elementwise pass, so every lane gets the same x'_j.
+// The column owner of the K^T y' phase computes x'_j the same way, stores it
+// with the new K^T y' and the record of the next step (pack buffers follow the
+// instance's `cur`); the pending average updates move to the owners (rows in
+// K x', columns in K^T y').
+__device__ __forceinline__ float4 ld_pack(const float4* p) {
+    float4 v;
+    asm volatile("ld.global.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ float primal_from_pack(const float4& r, float tau) {
+    return fminf(fmaxf(fmaf(-tau, r.y, r.x), r.z), r.w);
+}
+
+struct DualStepEpiPacked : DualStepEpi {
+    static constexpr bool kPackedX = true;
+    const float4* pack;  // records of the current point
+    float tau, w;        // the step's primal step size and average weight (StepScalars)
+    int avg;
+    __device__ float gather_x(int j) const { return primal_from_pack(ld_pack(pack + j), tau); }
+    __device__ void apply(int i, const SegDot<1>& d, const Pre& p) {
+        if (avg) V.y_acc[i] = ff_axpy(V.y_acc[i], w, p.y);
+        DualStepEpi::apply(i, d, p);
+    }
+};
+
+struct KtyStepEpiPacked {
+    static constexpr bool kCoherent = true;  // y' is written inside the launch
+    Vecs V;
+    const float4* pack;  // records of the current point
+    float4* pack_next;   // records of the candidate point (the other buffer)
+    const float *yg, *kty;
+    float *xn, *ktyn;
+    float tau, w;
+    int avg;
+    Acc inter, dx2;
+    struct Pre { float4 r; float kty, c; };
+    __device__ Pre pre(int j) const { return Pre{ld_pack(pack + j), kty[j], V.c[j]}; }
+    __device__ void begin(const Inst& S) {
+        yg = pick(V.y0, V.y1, S.cur ^ 1);
+        kty = pick(V.kty0, V.kty1, S.cur);
+        ktyn = pick(V.kty0, V.kty1, S.cur ^ 1);
+        xn = pick(V.x0, V.x1, S.cur ^ 1);
+    }
+    __device__ const float* gather(int) const { return yg; }
+    __device__ void apply(int j, const SegDot<1>& d, const Pre& p) {
+        const float k = d.f(0);
+        const float x = p.r.x, xp = primal_from_pack(p.r, tau);
+        if (avg) V.x_acc[j] = ff_axpy(V.x_acc[j], w, x);
+        xn[j] = xp;
+        ktyn[j] = k;
+        pack_next[j] = make_float4(xp, p.c + k, p.r.z, p.r.w);
+        const float dx = xp - x;
+        inter.add(dx * (k - p.kty));
+        dx2.add(dx * dx);
+    }
+    __device__ void values(Acc (&q)[2]) {
+        q[0] = inter;
+        q[1] = dx2;
+        inter.reset();
+        dx2.reset();
+    }
+    __device__ void finish(Inst&, const double*) {}
+};
 __global__ void __launch_bounds__(kSoloThreads, 1)
-    k_solo_steps(int nsteps, int N, int M, Side rows, Side cols, Vecs V, Inst* st, GridBar gb, float2* part) {
+    k_solo_steps(int nsteps, int N, Side rows, Side cols, Vecs V, Inst* st, GridBar gb, float2* part, float4* pack) {
     __shared__ Inst S;
     __shared__ StepScalars sc;
     __shared__ Acc red[(kSoloThreads / 32) * 2];
@@ -483,6 +553,7 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
     if (threadIdx.x == 0) {
         S = st[0];
         sc = step_scalars(S);
+        schedule_pows(S, V);
     }
     unsigned long long gen = grid_start(gb);
     __syncthreads();
@@ -490,30 +561,21 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
     float2* part_rows = part;          // [P] dy2
     float2* part_cols = part + 2 * P;  // [P][2] inter, dx2
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    // records of the current point (the evaluation between launches may have
+    // moved it: a restart to the average)
+    {
+        const int c = S.cur;
+        const float* x = pick(V.x0, V.x1, c);
+        const float* kt = pick(V.kty0, V.kty1, c);
+        float4* pk = pack + (size_t)c * N;
+        for (int j = tid; j < N; j += nthreads) pk[j] = make_float4(x[j], V.c[j] + kt[j], V.l[j], V.u[j]);
+    }
+    if (!grid_barrier(gb, gen)) return;
     for (int k = 0; k < nsteps && !S.done; ++k) {
-        // phase 1: pending average update, x' = clip(x - tau (c + K^T y), l, u)
+        const StepScalars s = sc;
+        // K x' (x' computed by the gathering lanes) and the dual step; sum |dy|^2
         {
-            const StepScalars s = sc;
-            const float* xs = pick(V.x0, V.x1, s.cur);
-            const float* kt = pick(V.kty0, V.kty1, s.cur);
-            float* xn = pick(V.x0, V.x1, s.cur ^ 1);
-            for (int j = tid; j < N; j += nthreads) {
-                const float xv = xs[j];
-                if (s.avg) V.x_acc[j] = ff_axpy(V.x_acc[j], s.w, xv);
-                const float v = fmaf(-s.tau, V.c[j] + kt[j], xv);
-                xn[j] = fminf(fmaxf(v, V.l[j]), V.u[j]);
-            }
-            if (s.avg) {
-                const float* ys = pick(V.y0, V.y1, s.cur);
-                for (int i = tid; i < M; i += nthreads) V.y_acc[i] = ff_axpy(V.y_acc[i], s.w, ys[i]);
-            }
-            // the step-size schedule of this attempt, for the controller at the end of phase 3
-            if (threadIdx.x == blockDim.x - 32) schedule_pows(S, V);
-        }
-        if (!grid_barrier(gb, gen)) return;
-        // phase 2: K x' and the dual step; sum |dy|^2
-        {
-            DualStepEpiCoherent epi{{V}};
+            DualStepEpiPacked epi{{V}, pack + (size_t)s.cur * N, s.tau, s.w, s.avg};
             Acc q[1];
             solo_side<1>(rows, S, epi, q);
             solo_block_partial<1>(q, part_rows + blockIdx.x, red);
@@ -525,9 +587,12 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
             if (threadIdx.x == 0) S.dy2 = tot[0];
             __syncthreads();
         }
-        // phase 3: K^T y', interaction and movement terms, step controller
+        // K^T y', x' stored by the column owners, the next records, step terms
         {
-            KtyStepEpiCoherent epi{{V}};
+            KtyStepEpiPacked epi{V, pack + (size_t)s.cur * N, pack + (size_t)(s.cur ^ 1) * N};
+            epi.tau = s.tau;
+            epi.w = s.w;
+            epi.avg = s.avg;
             Acc q[2];
             solo_side<2>(cols, S, epi, q);
             solo_block_partial<2>(q, part_cols + 2 * blockIdx.x, red);
@@ -539,6 +604,7 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
             if (threadIdx.x == 0) {
                 step_controller(S, tot[1], tot[0]);
                 sc = step_scalars(S);
+                schedule_pows(S, V);  // the next attempt's step-size schedule factors
             }
             __syncthreads();
         }
@@ -1541,6 +1607,7 @@ int MixedSolver::setup_persistent() {
         }
         SIHG_TRY(bar_.alloc(4 * sizeof(unsigned)));
         SIHG_TRY(part_.alloc(sizeof(float2) * 4 * (size_t)std::max(1, grid_form2_)));
+        if (B_ == 1) SIHG_TRY(pack_.alloc(sizeof(float4) * 2 * (size_t)std::max(1, N_)));
     }
     int form = opts_.persistent;
     if (form < 0) {
@@ -1589,8 +1656,8 @@ int MixedSolver::launch_persistent(cudaStream_t s, int nsteps) {
     const GridBar gb = make_bar(bar_, (unsigned)pgrid_, kBarrierLimitSec);
     if (persistent_ == 2) {
         cfg.blockDim = dim3((unsigned)kSoloThreads);
-        SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_solo_steps, nsteps, N_, M_, rows_, cols_, V_, state_.as<Inst>(), gb,
-                                     part_.as<float2>()));
+        SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_solo_steps, nsteps, N_, rows_, cols_, V_, state_.as<Inst>(), gb,
+                                     part_.as<float2>(), pack_.as<float4>()));
     } else {
         SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_steps_persistent, B_, nsteps, chunks_all_, rows_, cols_, V_,
                                      state_.as<Inst>(), gb));

@@ -220,7 +220,7 @@ class MixedSolver {
     // resident) and the grid barrier's words {arrive, gen, status}
     // (1 = the task-engine form, 2 = the single-LP form with per-block partials)
     int persistent_ = 0, pgrid_ = 0, grid_form1_ = 0, grid_form2_ = 0;
-    DevMem bar_, part_;
+    DevMem bar_, part_, pack_;
     // lanes per segment of the light tasks (0 = length rule), staged prefixes
     // the rule chose (the tuner may switch them off), tuned flag
     int lanes_r_ = 0, lanes_c_ = 0, stage_x_rule_ = 0, stage_y_rule_ = 0, tuned_ = 0;

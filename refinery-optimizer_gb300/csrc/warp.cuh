@@ -85,9 +85,23 @@ struct Coherent<Epi, decltype(void(Epi::kCoherent))> {
     static constexpr bool value = Epi::kCoherent;
 };
 
+// Computed gathers.  An epilogue with `kPackedX = true` supplies the gathered
+// value itself (`gather_x(idx)`), e.g. the primal step x'_j computed from a
+// packed per-column record, instead of a load from a vector.
+template <class Epi, class = void>
+struct PackedX {
+    static constexpr bool value = false;
+};
+template <class Epi>
+struct PackedX<Epi, decltype(void(Epi::kPackedX))> {
+    static constexpr bool value = Epi::kPackedX;
+};
+
 template <class Epi>
 __device__ __forceinline__ float gather_one(const Epi& epi, const float* __restrict__ vec, int idx) {
-    if constexpr (Coherent<Epi>::value) {
+    if constexpr (PackedX<Epi>::value) {
+        return epi.gather_x(idx);
+    } else if constexpr (Coherent<Epi>::value) {
         float v;
         asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(vec + idx));
         return v;
