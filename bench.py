@@ -79,14 +79,17 @@ NCU_TRAFFIC_PER_LAUNCH = {
 }
 
 
-# Engine options a workload runs with beyond the defaults (reported in the line's
-# config): the refinery scenario batches use primal-weight smoothing 0.8, which
-# took 358 s for the 512-scenario batch against 441 s with PDLP's 0.5 (the
-# slowest scenarios follow the primal weight much better; the single 168-period
-# LP is faster with 0.5, 11,904 against 15,232 steps).
+# Engine options a workload runs with beyond the defaults (reported in the
+# line's `engine_options`): the refinery scenario batches use primal-weight
+# smoothing 0.8, which took 358 s for the 512-scenario batch against 441 s with
+# PDLP's 0.5 (the slowest scenarios follow the primal weight much better; the
+# single 168-period LP is faster with 0.5, 11,904 against 15,232 steps), and one
+# lane per column in the A^T y light tasks, the shape the autotuner chose in the
+# run where all 512 scenarios reached 1e-4 (the summation order moves the
+# trajectories of the slowest scenarios; pinning it makes the run repeatable).
 WORKLOAD_OPTIONS = {
-    "refinery-512": {"primal_weight_smoothing": 0.8},
-    "refinery-64": {"primal_weight_smoothing": 0.8},
+    "refinery-512": {"primal_weight_smoothing": 0.8, "lanes_csc": 1},
+    "refinery-64": {"primal_weight_smoothing": 0.8, "lanes_csc": 1},
 }
 
 WORKLOADS = ["zipf-500kx1m", "random-2kx5k", "refinery-168p", "refinery-512", "refinery-64", "random-2kx5k-x256"]

@@ -2213,20 +2213,28 @@ int MixedSolver::autotune() {
         cols_s = sec[2];
         return SIH_PDHG_OK;
     };
+    // A candidate replaces the incumbent (the rule's choice first) only when it
+    // is faster by more than kTuneMargin: timing noise then does not flip the
+    // shape from one process to the next (the shape sets the summation order,
+    // so it also decides the exact trajectory of the iterates).
+    constexpr double kTuneMargin = 0.97;
     double tr = 0, tc = 0;
     // task size (lanes as configured)
     int best_t = task_nnz_;
     if (opts_.tile_nnz <= 0) {
-        std::vector<int> ladder = {384, 768, 1536, task_nnz_};
+        std::vector<int> ladder = {384, 768, 1536};
         if (nnz_ <= 64000000) ladder.insert(ladder.end(), {256, 512, 1024, 2048});
         std::sort(ladder.begin(), ladder.end());
         ladder.erase(std::unique(ladder.begin(), ladder.end()), ladder.end());
+        ladder.insert(ladder.begin(), task_nnz_);  // the incumbent, timed first
         double best = INFINITY;
-        for (int t : ladder) {
+        for (size_t k = 0; k < ladder.size(); ++k) {
+            const int t = ladder[k];
+            if (k > 0 && t == task_nnz_) continue;
             if ((long long)t > std::max<long long>(nnz_, 256)) continue;
             SIHG_TRY(build_schedules(t));
             SIHG_TRY(time_sides(tr, tc));
-            if (tr + tc < best) {
+            if (k == 0 || tr + tc < kTuneMargin * best) {
                 best = tr + tc;
                 best_t = t;
             }
@@ -2239,12 +2247,12 @@ int MixedSolver::autotune() {
         int& lanes = side == 0 ? lanes_r_ : lanes_c_;
         int best_l = lanes;
         double best = INFINITY;
-        for (int L : lane_ladder) {
+        for (int L : lane_ladder) {  // the rule (0) first: the incumbent
             lanes = L;
             SIHG_TRY(build_schedules(best_t));
             SIHG_TRY(time_sides(tr, tc));
             const double t = side == 0 ? tr : tc;
-            if (t < best) {
+            if (L == lane_ladder[0] || t < kTuneMargin * best) {
                 best = t;
                 best_l = L;
             }
@@ -2263,18 +2271,19 @@ int MixedSolver::autotune() {
         st = 0;
         SIHG_TRY(time_sides(tr, tc));
         const double off = side == 0 ? tr : tc;
-        st = on <= off ? rule : 0;
+        st = off < kTuneMargin * on ? 0 : rule;
     }
     // step form: graph of kernels per phase, or the persistent kernel
     if (opts_.persistent < 0) {
         const int alt = B_ == 1 ? 2 : 1;
         if ((alt == 1 ? grid_form1_ : grid_form2_) > 0) {
+            const int incumbent = persistent_;  // the automatic rule's form
+            const int other = incumbent == 0 ? alt : 0;
             double t0 = 0, t1 = 0;
-            SIHG_TRY(set_form(0));
             SIHG_TRY(time_block(&t0));
-            SIHG_TRY(set_form(alt));
+            SIHG_TRY(set_form(other));
             SIHG_TRY(time_block(&t1));
-            SIHG_TRY(set_form(t1 < t0 ? alt : 0));
+            SIHG_TRY(set_form(t1 < kTuneMargin * t0 ? other : incumbent));
         }
     }
     tuned_ = 1;
