@@ -107,7 +107,8 @@ if torch is not None:
         v* = c^T x* the optimal value of each instance."""
 
         @staticmethod
-        def forward(ctx, c, row_lower, row_upper, col_lower, col_upper, mats, config, adjoint_tol, certify_tol):
+        def forward(ctx, c, row_lower, row_upper, col_lower, col_upper, mats, config, adjoint_tol, certify_tol,
+                    polish=True):
             host = [t.detach().to("cpu", torch.float64).numpy() for t in (c, row_lower, row_upper, col_lower,
                                                                             col_upper)]
             probs = _problems(mats, *host)
@@ -115,10 +116,14 @@ if torch is not None:
             for i, s in enumerate(sols):
                 if not s.is_optimal():
                     raise RuntimeError(f"LP layer: instance {i} stopped with status {s.status.name}")
-            # the vertex of the identified basis: the point the adjoint differentiates
-            xp, yp, infos = polish_batch(probs, [s.x for s in sols], [s.row_duals for s in sols],
-                                         tolerance=adjoint_tol)
-            xs, ys, bad = choose_outputs(sols, xp, yp, infos, certify_tol)
+            if polish:
+                # the vertex of the identified basis: the point the adjoint differentiates
+                xp, yp, infos = polish_batch(probs, [s.x for s in sols], [s.row_duals for s in sols],
+                                             tolerance=adjoint_tol)
+                xs, ys, bad = choose_outputs(sols, xp, yp, infos, certify_tol)
+            else:  # the PDHG points as they are (optimal values and their gradients need no basis)
+                xs, ys = [s.x for s in sols], [s.row_duals for s in sols]
+                infos, bad = None, []
             if bad:
                 worst = max(max(infos[i]["primal_violation"], infos[i]["dual_violation"]) for i in bad)
                 warnings.warn(f"LP layer: {len(bad)} of {len(probs)} polished bases not optimal (worst relative "
@@ -152,20 +157,23 @@ if torch is not None:
                     out[k] += gv[:, None] * np.stack([d[k] for d in ctx.obj_grads])
             to_t = lambda k: torch.from_numpy(out[k]).to(ctx.device)
             return (to_t("c"), to_t("row_lower"), to_t("row_upper"), to_t("col_lower"), to_t("col_upper"),
-                    None, None, None, None)
+                    None, None, None, None, None)
 
     def lp_layer(mats: List[SparseMatrix], c, row_lower, row_upper, col_lower, col_upper,
                  config: Optional[GpuPdhgConfig] = None, adjoint_tol: float = 1e-6, certify_tol: float = 1e-6,
-                 return_objective: bool = False):
+                 return_objective: bool = False, polish: bool = True):
         """x* of each LP of the batch (a (batch, n) float64 tensor), differentiable
         with respect to the bounds (and c, with a zero implicit part).  Instances
         whose polished vertex is not certified within ``certify_tol`` return their
         PDHG point (with an LPLayerWarning).  With return_objective, also the
         optimal values v* = c^T x* (a (batch,) tensor) whose gradients come from
         the duals (objective_gradients): write an objective term of a loss as
-        v* rather than c^T x* to differentiate it without the basis."""
+        v* rather than c^T x* to differentiate it without the basis.  polish=False
+        skips the basis polish (the PDHG points are returned as they are): for
+        losses of v* alone, whose gradients need no basis, the layer is then one
+        batched solve."""
         cfg = config if config is not None else GpuPdhgConfig(max_iterations=1_000_000, tol_primal=1e-6,
                                                                tol_dual=1e-6, tol_gap=1e-6)
         x, v = LPFunction.apply(c, row_lower, row_upper, col_lower, col_upper, list(mats), cfg, adjoint_tol,
-                                certify_tol)
+                                certify_tol, polish)
         return (x, v) if return_objective else x

@@ -40,7 +40,7 @@ def test_layer_objective_gradient_is_the_simplex_dual(sih):
         c, rl, ru, l, u = (t(p.c), t(p.row_lower), t(p.row_upper), t(p.col_lower), t(p.col_upper))
         x, v = lp_layer([p.A], c, rl, ru, l, u, return_objective=True)
         ref = entry["highs_objective"]
-        assert float(v[0]) == pytest.approx(ref, rel=1e-5)
+        assert float(v[0].detach()) == pytest.approx(ref, rel=1e-5)
         v.sum().backward()
         db = (rl.grad + ru.grad).numpy()[0]
         y_highs = vec["highs/row_duals"] if "highs/row_duals" in vec.files else None
@@ -72,3 +72,25 @@ def test_layer_size_objective_gradient_matches_fp64_duals(sih):
               f"objective {g['objective']:.10g} vs {float(ref[f'obj{s}']):.10g}")
         assert err <= 1e-3
         assert g["objective"] == pytest.approx(float(ref[f"obj{s}"]), rel=2e-6)
+
+
+def test_layer_size_value_gradients_through_torch_without_polish(sih):
+    """The torch layer at the layer's size, polish off: one batched solve
+    forward, the optimal values' gradients (duals) backward; d v / d b against
+    the FP64 duals of the fixture."""
+    torch = pytest.importorskip("torch")
+    from sih_pdhg.generators import layer_lp
+    from sih_pdhg.layer import lp_layer
+
+    ref = np.load(os.path.join(GOLDEN, "layer_duals.npz"))
+    probs = [layer_lp(s) for s in (0, 1)]
+    st = lambda k: torch.tensor(np.stack([getattr(p, k) for p in probs]), dtype=torch.float64, requires_grad=True)
+    c, rl, ru, l, u = st("c"), st("row_lower"), st("row_upper"), st("col_lower"), st("col_upper")
+    x, v = lp_layer([p.A for p in probs], c, rl, ru, l, u, return_objective=True, polish=False)
+    v.sum().backward()
+    db = (rl.grad + ru.grad).numpy()
+    for k in range(2):
+        y = ref[f"y{k}"].astype(np.float64)
+        assert np.linalg.norm(db[k] - y) / np.linalg.norm(y) <= 1e-3
+        assert float(v[k].detach()) == pytest.approx(float(ref[f"obj{k}"]), rel=2e-6)
+    np.testing.assert_allclose(c.grad.numpy(), x.detach().numpy())
