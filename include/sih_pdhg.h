@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define SIH_PDHG_ABI_VERSION 1
+#define SIH_PDHG_ABI_VERSION 2
 
 /* ---- status codes of the ABI ------------------------------------------- */
 enum {
@@ -147,6 +147,14 @@ typedef struct sih_pdhg_options {
                                   0 = one kernel per phase, replayed as CUDA graphs; -1 = automatic (default):
                                   form 2 for one LP whose matrix fits in half of L2, the autotuner's choice
                                   when it runs, else 0. */
+    int32_t packed;            /* mixed, kernels per phase: 1 = two kernels per step, the elementwise primal
+                                  step folded into the SpMVs (the lanes that gather x' compute it from a packed
+                                  16-byte record per column; the column owners store it); same iterates as the
+                                  three-kernel step, but slower where measured (the 16-byte gathers cost more
+                                  than the elementwise pass: 500k x 1M LP 0.439 -> 0.516 s, 64 refinery
+                                  scenarios 47.9 -> 63.8 s).  0 = three kernels (default); staged gathers are
+                                  not used with 1.  The single-LP persistent form always works this way. */
+    int32_t reserved2;         /* 0 */
 } sih_pdhg_options;
 
 /*
@@ -261,6 +269,8 @@ typedef struct sih_pdhg_launch_shape {
     int32_t persistent; /* step form: 0 kernels per phase (graphs), 1 / 2 persistent (options.persistent) */
     int32_t grid;       /* blocks of the step SpMV launches */
     int32_t tuned;      /* 1 when the autotuner chose the shape */
+    int32_t packed;     /* 1: two kernels per step (options.packed) */
+    int32_t reserved;
 } sih_pdhg_launch_shape;
 int sih_pdhg_get_launch_shape(const sih_pdhg_handle* h, sih_pdhg_launch_shape* shape);
 void sih_pdhg_destroy(sih_pdhg_handle* h);

@@ -153,6 +153,7 @@ void sih_pdhg_options_default(sih_pdhg_options* o) {
     o->staged_kib = 0;
     o->autotune = -1;
     o->persistent = -1;
+    o->packed = 0;
     o->verbose = 0;
     o->time_limit_sec = 0.0;
     o->restart_sufficient = 0.2;

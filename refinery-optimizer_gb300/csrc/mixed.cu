@@ -496,9 +496,19 @@ __device__ __forceinline__ float primal_from_pack(const float4& r, float tau) {
 
 struct DualStepEpiPacked : DualStepEpi {
     static constexpr bool kPackedX = true;
-    const float4* pack;  // records of the current point
-    float tau, w;        // the step's primal step size and average weight (StepScalars)
+    const float4* pack_base;  // [2 N] records, one buffer per `cur`
+    int ncols;                // N, columns of the whole batch
+    const float4* pack;       // records of the instance's current point
+    float tau, w;             // the primal step size and average weight, as step_scalars computes them
     int avg;
+    __device__ void begin(const Inst& S) {
+        DualStepEpi::begin(S);
+        const StepScalars sc = step_scalars(S);
+        tau = sc.tau;
+        w = sc.w;
+        avg = sc.avg;
+        pack = pack_base + (size_t)S.cur * ncols;
+    }
     __device__ float gather_x(int j) const { return primal_from_pack(ld_pack(pack + j), tau); }
     __device__ void apply(int i, const SegDot<1>& d, const Pre& p) {
         if (avg) V.y_acc[i] = ff_axpy(V.y_acc[i], w, p.y);
@@ -506,9 +516,13 @@ struct DualStepEpiPacked : DualStepEpi {
     }
 };
 
+// COHERENT: y' was written inside the same launch (the persistent form).
+template <bool COHERENT>
 struct KtyStepEpiPacked {
-    static constexpr bool kCoherent = true;  // y' is written inside the launch
+    static constexpr bool kCoherent = COHERENT;
     Vecs V;
+    float4* pack_base;
+    int ncols;
     const float4* pack;  // records of the current point
     float4* pack_next;   // records of the candidate point (the other buffer)
     const float *yg, *kty;
@@ -519,6 +533,12 @@ struct KtyStepEpiPacked {
     struct Pre { float4 r; float kty, c; };
     __device__ Pre pre(int j) const { return Pre{ld_pack(pack + j), kty[j], V.c[j]}; }
     __device__ void begin(const Inst& S) {
+        const StepScalars sc = step_scalars(S);
+        tau = sc.tau;
+        w = sc.w;
+        avg = sc.avg;
+        pack = pack_base + (size_t)S.cur * ncols;
+        pack_next = pack_base + (size_t)(S.cur ^ 1) * ncols;
         yg = pick(V.y0, V.y1, S.cur ^ 1);
         kty = pick(V.kty0, V.kty1, S.cur);
         ktyn = pick(V.kty0, V.kty1, S.cur ^ 1);
@@ -542,17 +562,51 @@ struct KtyStepEpiPacked {
         inter.reset();
         dx2.reset();
     }
-    __device__ void finish(Inst&, const double*) {}
+    // the instance's step-size controller (task engine; the single-LP form runs
+    // it itself after its grid reduction)
+    __device__ void finish(Inst& S, const double* tot) { step_controller(S, tot[1], tot[0]); }
 };
+
+// Kernel-per-phase packed steps (options.packed): two kernels per step, the
+// elementwise primal pass folded into them as in the single-LP form.  Same
+// operations on the same values as the three-kernel step, so the iterates are
+// bit-identical; the step moves the x' / average traffic of the elementwise
+// pass into the two SpMV kernels.  Measured slower than the three kernels on
+// bandwidth-bound LPs (a 16-byte record per gathered column costs more than
+// the elementwise pass saves), so it is an option, off by default.
+__global__ void __launch_bounds__(kThreads, 4)
+    k_step_dual_packed(int B, Side rows, Vecs V, Inst* __restrict__ st, const float4* __restrict__ pack, int N) {
+    chain_wait();
+    step_schedule_pows(B, st, V);
+    DualStepEpiPacked epi{{V}, pack, N};
+    spmv_engine<1, true, 1>(rows, st, epi, 0u);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) k_step_kty_packed(Side cols, Vecs V, Inst* __restrict__ st, float4* pack,
+                                                                 int N) {
+    chain_wait();
+    KtyStepEpiPacked<false> epi{V, pack, N};
+    spmv_engine<1, true, 2>(cols, st, epi, 0u);
+}
+
+// Records of every running instance's current point (after an evaluation,
+// which may restart an instance at its average point).
+__global__ void __launch_bounds__(kThreads) k_pack(Chunks ch, Vecs V, Inst* __restrict__ st, float4* pack, int N) {
+    for_each_element(ch, st, step_scalars, [&](bool is_col, const StepScalars& S, int r) {
+        if (!is_col) return;
+        const float x = pick(V.x0, V.x1, S.cur)[r];
+        const float kt = pick(V.kty0, V.kty1, S.cur)[r];
+        pack[(size_t)S.cur * N + r] = make_float4(x, V.c[r] + kt, V.l[r], V.u[r]);
+    });
+}
+
 __global__ void __launch_bounds__(kSoloThreads, 1)
     k_solo_steps(int nsteps, int N, Side rows, Side cols, Vecs V, Inst* st, GridBar gb, float2* part, float4* pack) {
     __shared__ Inst S;
-    __shared__ StepScalars sc;
     __shared__ Acc red[(kSoloThreads / 32) * 2];
     if (ld_status(gb.status) != 0) return;
     if (threadIdx.x == 0) {
         S = st[0];
-        sc = step_scalars(S);
         schedule_pows(S, V);
     }
     unsigned long long gen = grid_start(gb);
@@ -572,10 +626,9 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
     }
     if (!grid_barrier(gb, gen)) return;
     for (int k = 0; k < nsteps && !S.done; ++k) {
-        const StepScalars s = sc;
         // K x' (x' computed by the gathering lanes) and the dual step; sum |dy|^2
         {
-            DualStepEpiPacked epi{{V}, pack + (size_t)s.cur * N, s.tau, s.w, s.avg};
+            DualStepEpiPacked epi{{V}, pack, N};
             Acc q[1];
             solo_side<1>(rows, S, epi, q);
             solo_block_partial<1>(q, part_rows + blockIdx.x, red);
@@ -589,10 +642,7 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
         }
         // K^T y', x' stored by the column owners, the next records, step terms
         {
-            KtyStepEpiPacked epi{V, pack + (size_t)s.cur * N, pack + (size_t)(s.cur ^ 1) * N};
-            epi.tau = s.tau;
-            epi.w = s.w;
-            epi.avg = s.avg;
+            KtyStepEpiPacked<true> epi{V, pack, N};
             Acc q[2];
             solo_side<2>(cols, S, epi, q);
             solo_block_partial<2>(q, part_cols + 2 * blockIdx.x, red);
@@ -603,7 +653,6 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
             solo_grid_total<2>(part_cols, P, tot, red);
             if (threadIdx.x == 0) {
                 step_controller(S, tot[1], tot[0]);
-                sc = step_scalars(S);
                 schedule_pows(S, V);  // the next attempt's step-size schedule factors
             }
             __syncthreads();
@@ -1584,8 +1633,18 @@ int MixedSolver::setup(const std::vector<const HostProblem*>& probs, const sih_p
     }
     phase("state");
     SIHG_TRY(setup_persistent());
+    SIHG_TRY(setup_packed());
     // autotune: 1 on, 0 off, < 0 automatic (on for batches)
     if (opts.autotune > 0 || (opts.autotune < 0 && B_ > 1)) SIHG_TRY(autotune());
+    return SIH_PDHG_OK;
+}
+
+// Packed kernel-per-phase steps (options.packed, off by default: slower where
+// measured); the single-LP persistent form always works on the records.
+int MixedSolver::setup_packed() {
+    packed_ = opts_.packed > 0 ? 1 : 0;
+    if ((packed_ || B_ == 1) && pack_.bytes() < sizeof(float4) * 2 * (size_t)std::max(1, N_))
+        SIHG_TRY(pack_.alloc(sizeof(float4) * 2 * (size_t)std::max(1, N_)));
     return SIH_PDHG_OK;
 }
 
@@ -1607,7 +1666,6 @@ int MixedSolver::setup_persistent() {
         }
         SIHG_TRY(bar_.alloc(4 * sizeof(unsigned)));
         SIHG_TRY(part_.alloc(sizeof(float2) * 4 * (size_t)std::max(1, grid_form2_)));
-        if (B_ == 1) SIHG_TRY(pack_.alloc(sizeof(float4) * 2 * (size_t)std::max(1, N_)));
     }
     int form = opts_.persistent;
     if (form < 0) {
@@ -1715,9 +1773,11 @@ static cudaError_t launch_chained(void (*kernel)(P...), int grid, int block, siz
 }
 
 int MixedSolver::launch_step(cudaStream_t s) {
-    launches_ += 3;
     Inst* st = state_.as<Inst>();
-    SIHG_CUDA(launch_chained(k_step_primal, elem_grid_, kThreads, 0, s, B_, chunks_all_, V_, st));
+    if (!packed_) {
+        launches_ += 1;
+        SIHG_CUDA(launch_chained(k_step_primal, elem_grid_, kThreads, 0, s, B_, chunks_all_, V_, st));
+    }
     SIHG_TRY(launch_step_spmvs(s, 1));
     SIHG_TRY(launch_step_spmvs(s, 2));
     SIHG_LAUNCH_CHECK();
@@ -1728,6 +1788,15 @@ int MixedSolver::launch_step(cudaStream_t s) {
 // the step-size controller), staged when choose_staging picked a prefix.
 int MixedSolver::launch_step_spmvs(cudaStream_t s, int which) {
     Inst* st = state_.as<Inst>();
+    launches_ += 1;
+    if (packed_) {
+        if (which == 1)
+            SIHG_CUDA(launch_chained(k_step_dual_packed, grid_, kThreads, 0, s, B_, rows_, V_, st,
+                                     (const float4*)pack_.as<float4>(), N_));
+        else
+            SIHG_CUDA(launch_chained(k_step_kty_packed, grid_, kThreads, 0, s, cols_, V_, st, pack_.as<float4>(), N_));
+        return SIH_PDHG_OK;
+    }
     if (which == 1) {
         if (stage_x_ > 0)
             SIHG_CUDA(launch_chained(k_step_dual_staged, sm_count_, kStagedThreads, sizeof(float) * stage_x_, s, B_,
@@ -1797,6 +1866,10 @@ int MixedSolver::launch_eval(cudaStream_t s) {
     k_eval_rows<<<grid_, kThreads, 0, s>>>(rows_, V_, st);
     k_eval_cols<<<grid_, kThreads, 0, s>>>(cols_, V_, st, done_count_.as<unsigned>());
     k_restart<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st);
+    if (packed_ && persistent_ == 0) {  // records of the (possibly restarted) current points
+        k_pack<<<elem_grid_, kThreads, 0, s>>>(chunks_all_, V_, st, pack_.as<float4>(), N_);
+        launches_ += 1;
+    }
     SIHG_LAUNCH_CHECK();
     return launch_compact(s);
 }
@@ -1932,7 +2005,7 @@ int MixedSolver::run() {
             } else if (graph) {
                 cudaError_t e = cudaGraphLaunch(graphs_[0], s);
                 if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch", __FILE__, __LINE__);
-                launches_ += 3ull * eval_freq_ + 6ull;
+                launches_ += (packed_ ? 2ull : 3ull) * eval_freq_ + (packed_ ? 7ull : 6ull);
             } else {
                 for (int j = 0; j < eval_freq_; ++j) SIHG_TRY(launch_step(s));
                 SIHG_TRY(launch_eval(s));
@@ -2058,6 +2131,7 @@ int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
         for (int i = 0; i < reps; ++i) {
             int r = SIH_PDHG_OK;
             if (k == 0) {
+                if (packed_) break;  // no elementwise kernel in the packed step
                 const cudaError_t e = launch_chained(k_step_primal, elem_grid_, kThreads, 0, s, B_, chunks_all_, V_, st);
                 if (e != cudaSuccess) r = cuda_fail(e, "k_step_primal launch", __FILE__, __LINE__);
             } else {
@@ -2073,16 +2147,24 @@ int MixedSolver::time_kernels(int reps, double* seconds, double* bytes) {
         if (e != cudaSuccess) rc = cuda_fail(e, "kernel timing", __FILE__, __LINE__);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        seconds[k] = ms * 1e-3 / reps;
+        seconds[k] = (k == 0 && packed_) ? 0.0 : ms * 1e-3 / reps;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (bytes) {
         // algorithmic bytes of one launch: every array the kernel must touch, once
         const double nnz = (double)nnz_, m = M_, n = N_;
-        bytes[0] = 40.0 * n + 20.0 * m;                   // x,K^T y,c,l,u in, x' out, x/y averages in+out
-        bytes[1] = 8.0 * nnz + 4.0 * (m + 1) + 4.0 * n + 28.0 * m;  // pairs, ptr, x' gathered, row epilogue
-        bytes[2] = 8.0 * nnz + 4.0 * (n + 1) + 4.0 * m + 16.0 * n;  // pairs, ptr, y' gathered, column epilogue
+        if (packed_) {
+            bytes[0] = 0.0;
+            // pairs, ptr, a 16-byte record per column gathered, row epilogue with the y average
+            bytes[1] = 8.0 * nnz + 4.0 * (m + 1) + 16.0 * n + 44.0 * m;
+            // pairs, ptr, y' gathered; per column: record, K^T y, c in; x', K^T y', record out; x average in+out
+            bytes[2] = 8.0 * nnz + 4.0 * (n + 1) + 4.0 * m + 60.0 * n;
+        } else {
+            bytes[0] = 40.0 * n + 20.0 * m;                   // x,K^T y,c,l,u in, x' out, x/y averages in+out
+            bytes[1] = 8.0 * nnz + 4.0 * (m + 1) + 4.0 * n + 28.0 * m;  // pairs, ptr, x' gathered, row epilogue
+            bytes[2] = 8.0 * nnz + 4.0 * (n + 1) + 4.0 * m + 16.0 * n;  // pairs, ptr, y' gathered, column epilogue
+        }
     }
     return rc;
 }
@@ -2149,6 +2231,8 @@ void MixedSolver::launch_shape(sih_pdhg_launch_shape* out) const {
     out->persistent = persistent_;
     out->grid = persistent_ ? pgrid_ : grid_;
     out->tuned = tuned_;
+    out->packed = packed_;
+    out->reserved = 0;
 }
 
 // A cached shape; what the caller's options fix stays as they say.

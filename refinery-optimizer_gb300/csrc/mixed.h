@@ -186,6 +186,7 @@ class MixedSolver {
     int launch_persistent(cudaStream_t s, int nsteps);
     int setup_persistent();
     int set_form(int form);
+    int setup_packed();
     int apply_shape(const sih_pdhg_launch_shape& sh);
     int time_block(double* seconds);
 
@@ -224,6 +225,7 @@ class MixedSolver {
     // lanes per segment of the light tasks (0 = length rule), staged prefixes
     // the rule chose (the tuner may switch them off), tuned flag
     int lanes_r_ = 0, lanes_c_ = 0, stage_x_rule_ = 0, stage_y_rule_ = 0, tuned_ = 0;
+    int packed_ = 0;  // options.packed: two kernels per step on packed column records
     Vecs V_{};
     std::vector<Inst> host_inst_;
     std::vector<std::vector<float>> start_x_, start_y_;  // warm starts (device order, unscaled)

@@ -17,7 +17,7 @@ PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.environ.get("SIH_PDHG_LIB") or os.path.join(PKG_DIR, "_build", "libsih_pdhg.so")
 
 OK = 0
-ABI_VERSION = 1  # SIH_PDHG_ABI_VERSION of include/sih_pdhg.h that these ctypes layouts mirror
+ABI_VERSION = 2  # SIH_PDHG_ABI_VERSION of include/sih_pdhg.h that these ctypes layouts mirror
 ERR_NAMES = {1: "invalid argument", 2: "no CUDA device", 3: "CUDA error", 4: "out of memory", 5: "unsupported"}
 
 ALGO_PLAIN = 0
@@ -48,13 +48,13 @@ class COptions(C.Structure):
                 ("primal_weight_smoothing", C.c_double), ("exact_arithmetic", C.c_int32),
                 ("lanes_csr", C.c_int32), ("lanes_csc", C.c_int32), ("heavy_factor", C.c_int32),
                 ("tile_nnz", C.c_int32), ("reorder", C.c_int32), ("staged_kib", C.c_int32),
-                ("persistent", C.c_int32)]
+                ("persistent", C.c_int32), ("packed", C.c_int32), ("reserved2", C.c_int32)]
 
 
 class CLaunchShape(C.Structure):
     _fields_ = [("task_nnz", C.c_int32), ("row_lanes", C.c_int32), ("col_lanes", C.c_int32),
                 ("staged_x", C.c_int32), ("staged_y", C.c_int32), ("persistent", C.c_int32), ("grid", C.c_int32),
-                ("tuned", C.c_int32)]
+                ("tuned", C.c_int32), ("packed", C.c_int32), ("reserved", C.c_int32)]
 
 
 class CAdjointOptions(C.Structure):

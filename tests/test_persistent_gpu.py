@@ -138,3 +138,30 @@ def test_automatic_form_and_launch_shape(sih):
     assert all(r.is_optimal() for r in res)
     with sih.PdhgHandle(batch, cfg(sih), algorithm=sih.ALGO_MIXED) as h:
         assert h.launch_shape() == sh
+
+
+def test_packed_steps_equal_three_kernel_steps(sih):
+    """options.packed: two kernels per step (the elementwise primal step folded
+    into the SpMVs, x' computed from packed column records) give the iterates
+    of the three-kernel step bit for bit, on a single LP and on a batch whose
+    instances restart and stop at different evaluations."""
+    from sih_pdhg.generators import mixed_bounds_lp, refinery_lp, small_random_lp
+
+    prob, _, _ = golden_case("rand_2000x5000_k8_s0")
+    kw = dict(persistent=0, autotune=0, staged_kib=-1)
+    a = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6), packed=0, **kw)
+    b = sih.solve_gpu_mixed(prob, cfg(sih, 1e-6), packed=1, **kw)
+    assert a.is_optimal() and a.simplex_iterations == b.simplex_iterations and a.restarts == b.restarts
+    np.testing.assert_array_equal(a.x, b.x)
+    np.testing.assert_array_equal(a.row_duals, b.row_duals)
+    probs = [small_random_lp(300, 700, 6, 3), mixed_bounds_lp(seed=1), refinery_lp(24, 1), small_random_lp(50, 120, 4, 2)]
+    ra = sih.solve_batch(probs, cfg(sih), packed=0, **kw)
+    rb = sih.solve_batch(probs, cfg(sih), packed=1, **kw)
+    for x, y in zip(ra, rb):
+        assert x.status == y.status and x.simplex_iterations == y.simplex_iterations
+        np.testing.assert_array_equal(x.x, y.x)
+        np.testing.assert_array_equal(x.row_duals, y.row_duals)
+    with sih.PdhgHandle(probs, cfg(sih), algorithm=sih.ALGO_MIXED, packed=1, **kw) as h:
+        sh = h.launch_shape()
+        secs, byts = h.time_kernels(3)
+    assert sh["packed"] == 1 and secs[0] == 0.0 and secs[1] > 0 and secs[2] > 0
