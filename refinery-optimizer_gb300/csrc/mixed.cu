@@ -394,7 +394,7 @@ __global__ void __launch_bounds__(kThreads, 4)
 // barrier is needed; block 0 writes the state back when the launch ends.
 // Deterministic; the sums are grouped differently from the task engine's, so
 // the iterates agree with the other forms to rounding, not bit for bit.
-constexpr int kSoloThreads = 640;  // 20 warps per SM at 96 registers (measured best of 512 / 640 / 768 / 1024)
+constexpr int kSoloThreads = 640;  // 20 warps per SM at 96 registers (measured best of 640 / 768 / 1024)
 // Automatic step form: the single-LP form when the matrix (both sides) takes
 // at most this many bytes, half of the 129 MB L2 (measured per step: 80k
 // nonzeros 30.9 -> 20.8 us, 1.1M nonzeros 46.1 -> 38.8 us).
@@ -1712,14 +1712,26 @@ int MixedSolver::launch_persistent(cudaStream_t s, int nsteps) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     const GridBar gb = make_bar(bar_, (unsigned)pgrid_, kBarrierLimitSec);
+    cudaError_t e;
     if (persistent_ == 2) {
         cfg.blockDim = dim3((unsigned)kSoloThreads);
-        SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_solo_steps, nsteps, N_, rows_, cols_, V_, state_.as<Inst>(), gb,
-                                     part_.as<float2>(), pack_.as<float4>()));
+        e = cudaLaunchKernelEx(&cfg, k_solo_steps, nsteps, N_, rows_, cols_, V_, state_.as<Inst>(), gb,
+                               part_.as<float2>(), pack_.as<float4>());
     } else {
-        SIHG_CUDA(cudaLaunchKernelEx(&cfg, k_steps_persistent, B_, nsteps, chunks_all_, rows_, cols_, V_,
-                                     state_.as<Inst>(), gb));
+        e = cudaLaunchKernelEx(&cfg, k_steps_persistent, B_, nsteps, chunks_all_, rows_, cols_, V_,
+                               state_.as<Inst>(), gb);
     }
+    if (e == cudaErrorCooperativeLaunchTooLarge && opts_.persistent < 0) {
+        // the device cannot hold the whole grid at once now (SMs taken by other
+        // work, or a partitioned device): nothing was launched; with the step
+        // form left to the engine, these and all later steps run as kernels per
+        // phase instead
+        (void)cudaGetLastError();
+        SIHG_TRY(set_form(0));
+        for (int k = 0; k < nsteps; ++k) SIHG_TRY(launch_step(s));
+        return SIH_PDHG_OK;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "persistent step kernel launch", __FILE__, __LINE__);
     launches_ += 1;
     return SIH_PDHG_OK;
 }
