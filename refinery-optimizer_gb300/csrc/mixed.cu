@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(kThreads) k_pack(Chunks ch, Vecs V, Inst* __re
 __global__ void __launch_bounds__(kSoloThreads, 1)
     k_solo_steps(int nsteps, int N, Side rows, Side cols, Vecs V, Inst* st, GridBar gb, float2* part, float4* pack) {
     __shared__ Inst S;
-    __shared__ Acc red[(kSoloThreads / 32) * 2];
+    __shared__ Acc red[(kSoloThreads / 32) * 3];
     if (ld_status(gb.status) != 0) return;
     if (threadIdx.x == 0) {
         S = st[0];
@@ -611,9 +611,12 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
     }
     unsigned long long gen = grid_start(gb);
     __syncthreads();
+    // Block partials [2][P][3] (dy2, inter, dx2), double-buffered by step: the
+    // |dy|^2 partials of K x' are reduced together with the K^T y' partials
+    // after the step's last barrier (the controller is their only reader), and
+    // a block can be writing the next step's partials while a slower one still
+    // reads these.
     const int P = gridDim.x;
-    float2* part_rows = part;          // [P] dy2
-    float2* part_cols = part + 2 * P;  // [P][2] inter, dx2
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
     // records of the current point (the evaluation between launches may have
     // moved it: a restart to the average)
@@ -626,33 +629,29 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
     }
     if (!grid_barrier(gb, gen)) return;
     for (int k = 0; k < nsteps && !S.done; ++k) {
+        float2* pb = part + (size_t)(k & 1) * 3 * P;
         // K x' (x' computed by the gathering lanes) and the dual step; sum |dy|^2
         {
             DualStepEpiPacked epi{{V}, pack, N};
             Acc q[1];
             solo_side<1>(rows, S, epi, q);
-            solo_block_partial<1>(q, part_rows + blockIdx.x, red);
+            solo_block_partial<1>(q, pb + 3 * blockIdx.x, red);
         }
         if (!grid_barrier(gb, gen)) return;
-        {
-            double tot[1];
-            solo_grid_total<1>(part_rows, P, tot, red);
-            if (threadIdx.x == 0) S.dy2 = tot[0];
-            __syncthreads();
-        }
         // K^T y', x' stored by the column owners, the next records, step terms
         {
             KtyStepEpiPacked<true> epi{V, pack, N};
             Acc q[2];
             solo_side<2>(cols, S, epi, q);
-            solo_block_partial<2>(q, part_cols + 2 * blockIdx.x, red);
+            solo_block_partial<2>(q, pb + 3 * blockIdx.x + 1, red);
         }
         if (!grid_barrier(gb, gen)) return;
         {
-            double tot[2];
-            solo_grid_total<2>(part_cols, P, tot, red);
+            double tot[3];
+            solo_grid_total<3>(pb, P, tot, red);
             if (threadIdx.x == 0) {
-                step_controller(S, tot[1], tot[0]);
+                S.dy2 = tot[0];
+                step_controller(S, tot[2], tot[1]);
                 schedule_pows(S, V);  // the next attempt's step-size schedule factors
             }
             __syncthreads();
@@ -1665,7 +1664,7 @@ int MixedSolver::setup_persistent() {
             grid_form2_ = sm_count_ * occ;
         }
         SIHG_TRY(bar_.alloc(4 * sizeof(unsigned)));
-        SIHG_TRY(part_.alloc(sizeof(float2) * 4 * (size_t)std::max(1, grid_form2_)));
+        SIHG_TRY(part_.alloc(sizeof(float2) * 6 * (size_t)std::max(1, grid_form2_)));
     }
     int form = opts_.persistent;
     if (form < 0) {
