@@ -12,7 +12,7 @@ import pytest
 import oracle  # test infrastructure: locates the reference sources
 from conftest import REPO
 
-REF = oracle.reference_dir() or ""  # the reference sources, where present (this build's recipe knows where)
+REF = oracle.reference_dir() or ""  # the reference sources, where present (located by oracle/ref_build.sh)
 ENGINE_CORE = os.path.join(REPO, "oracle", "_ref", "engine")
 
 

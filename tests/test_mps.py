@@ -23,7 +23,7 @@ import oracle  # test infrastructure: locates the reference sources
 from conftest import GOLDEN, REPO
 
 MPS_DIR = os.path.join(GOLDEN, "mps")
-REF = oracle.reference_dir() or ""  # the reference sources, where present (this build's recipe knows where)
+REF = oracle.reference_dir() or ""  # the reference sources, where present (located by oracle/ref_build.sh)
 REF_CORE = os.path.join(REPO, "oracle", "_ref", "intended")
 ARRAYS = ("csc_col_ptr", "csc_row_ind", "csc_values", "csr_row_ptr", "csr_col_ind", "csr_values", "c", "col_lower",
           "col_upper", "row_lower", "row_upper")
