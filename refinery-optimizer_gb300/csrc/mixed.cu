@@ -501,12 +501,15 @@ struct DualStepEpiPacked : DualStepEpi {
     const float4* pack;       // records of the instance's current point
     float tau, w;             // the primal step size and average weight, as step_scalars computes them
     int avg;
+    int preset;               // 1: tau, w, avg were set by the caller (no FP64 division per warp)
     __device__ void begin(const Inst& S) {
         DualStepEpi::begin(S);
-        const StepScalars sc = step_scalars(S);
-        tau = sc.tau;
-        w = sc.w;
-        avg = sc.avg;
+        if (!preset) {
+            const StepScalars sc = step_scalars(S);
+            tau = sc.tau;
+            w = sc.w;
+            avg = sc.avg;
+        }
         pack = pack_base + (size_t)S.cur * ncols;
     }
     __device__ float gather_x(int j) const { return primal_from_pack(ld_pack(pack + j), tau); }
@@ -529,14 +532,17 @@ struct KtyStepEpiPacked {
     float *xn, *ktyn;
     float tau, w;
     int avg;
+    int preset;  // 1: tau, w, avg were set by the caller
     Acc inter, dx2;
     struct Pre { float4 r; float kty, c; };
     __device__ Pre pre(int j) const { return Pre{ld_pack(pack + j), kty[j], V.c[j]}; }
     __device__ void begin(const Inst& S) {
-        const StepScalars sc = step_scalars(S);
-        tau = sc.tau;
-        w = sc.w;
-        avg = sc.avg;
+        if (!preset) {
+            const StepScalars sc = step_scalars(S);
+            tau = sc.tau;
+            w = sc.w;
+            avg = sc.avg;
+        }
         pack = pack_base + (size_t)S.cur * ncols;
         pack_next = pack_base + (size_t)(S.cur ^ 1) * ncols;
         yg = pick(V.y0, V.y1, S.cur ^ 1);
@@ -603,10 +609,12 @@ __global__ void __launch_bounds__(kThreads) k_pack(Chunks ch, Vecs V, Inst* __re
 __global__ void __launch_bounds__(kSoloThreads, 1)
     k_solo_steps(int nsteps, int N, Side rows, Side cols, Vecs V, Inst* st, GridBar gb, float2* part, float4* pack) {
     __shared__ Inst S;
+    __shared__ StepScalars sc;  // the step's FP32 scalars, one FP64 division per block per step
     __shared__ Acc red[(kSoloThreads / 32) * 3];
     if (ld_status(gb.status) != 0) return;
     if (threadIdx.x == 0) {
         S = st[0];
+        sc = step_scalars(S);
         schedule_pows(S, V);
     }
     unsigned long long gen = grid_start(gb);
@@ -631,8 +639,9 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
     for (int k = 0; k < nsteps && !S.done; ++k) {
         float2* pb = part + (size_t)(k & 1) * 3 * P;
         // K x' (x' computed by the gathering lanes) and the dual step; sum |dy|^2
+        const StepScalars s = sc;
         {
-            DualStepEpiPacked epi{{V}, pack, N};
+            DualStepEpiPacked epi{{V}, pack, N, nullptr, s.tau, s.w, s.avg, 1};
             Acc q[1];
             solo_side<1>(rows, S, epi, q);
             solo_block_partial<1>(q, pb + 3 * blockIdx.x, red);
@@ -641,6 +650,10 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
         // K^T y', x' stored by the column owners, the next records, step terms
         {
             KtyStepEpiPacked<true> epi{V, pack, N};
+            epi.tau = s.tau;
+            epi.w = s.w;
+            epi.avg = s.avg;
+            epi.preset = 1;
             Acc q[2];
             solo_side<2>(cols, S, epi, q);
             solo_block_partial<2>(q, pb + 3 * blockIdx.x + 1, red);
@@ -652,6 +665,7 @@ __global__ void __launch_bounds__(kSoloThreads, 1)
             if (threadIdx.x == 0) {
                 S.dy2 = tot[0];
                 step_controller(S, tot[2], tot[1]);
+                sc = step_scalars(S);
                 schedule_pows(S, V);  // the next attempt's step-size schedule factors
             }
             __syncthreads();
