@@ -67,11 +67,11 @@ int upload_side(const SideSchedule& sc, int B, const SegMatrix& A, unsigned* tic
 
 int TaskLayout::build(const std::vector<int>& csr_ptr, const std::vector<int>& csc_ptr, const std::vector<int>& roff,
                       const std::vector<int>& coff, const SegMatrix& rows_A, const SegMatrix& cols_A, int task_nnz,
-                      bool all_active, cudaStream_t s, int row_lanes, int col_lanes) {
+                      bool all_active, cudaStream_t s, int row_lanes, int col_lanes, int max_segs) {
     const int B = (int)roff.size() - 1;
     SideSchedule rs, cs;
-    make_schedule(csr_ptr, roff, task_nnz, rs, row_lanes);
-    make_schedule(csc_ptr, coff, task_nnz, cs, col_lanes);
+    make_schedule(csr_ptr, roff, task_nnz, rs, row_lanes, max_segs);
+    make_schedule(csc_ptr, coff, task_nnz, cs, col_lanes, max_segs);
     // per side: tickets [B] + counters [2] + group tickets [ngroups], zeroed once;
     // the kernels leave the tickets zero
     const size_t ng_r = rs.group_begin.size() - 1, ng_c = cs.group_begin.size() - 1;

@@ -399,6 +399,13 @@ constexpr int kSoloThreads = 640;  // 20 warps per SM at 96 registers (measured 
 // at most this many bytes, half of the 129 MB L2 (measured per step: 80k
 // nonzeros 30.9 -> 20.8 us, 1.1M nonzeros 46.1 -> 38.8 us).
 constexpr double kSoloMaxBytes = 64.0 * 1024.0 * 1024.0;
+// Segments per light task on such an LP (the others keep kTaskSegs): a task's
+// lane groups walk its segments one pointer round trip per pass, so on an
+// L2-resident LP the tasks of short segments (128 columns of one nonzero at
+// 128 nonzeros per task) set a phase's slowest warp.  Single-LP persistent
+// form, per step: refinery 24 periods 16.2 -> 14.7 us, 168 periods
+// 28.0 -> 26.0 us (32 segments: 14.3 / 26.9 us).
+constexpr int kSoloTaskSegs = 64;
 
 template <int Q>
 __device__ __forceinline__ void solo_block_partial(Acc (&q)[Q], float2* __restrict__ out, Acc* sh) {
@@ -1236,6 +1243,10 @@ __global__ void k_compact_fill(int B, const Inst* __restrict__ st, Side rows, Si
 }
 
 // ---------------------------------------------------------------- host: schedule
+// Shortest run of long segments that a light task skips instead of walking:
+// one pass of 1-lane groups.
+constexpr int kSkipRun = 32;
+
 static int pow2_floor(int v) {
     int p = 1;
     while (p * 2 <= v) p *= 2;
@@ -1243,8 +1254,9 @@ static int pow2_floor(int v) {
 }
 
 void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out,
-                   int light_lanes) {
+                   int light_lanes, int max_segs) {
     if (light_lanes > 0) light_lanes = std::min(32, pow2_floor(light_lanes));
+    max_segs = std::max(1, std::min(kTaskSegs, max_segs));
     const int B = (int)inst_off.size() - 1;
     out = SideSchedule{};
     out.light_max.assign(B, 0);
@@ -1257,12 +1269,25 @@ void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off
         const int L0 = std::max(1, std::min(32, pow2_floor(std::max(1, mean / kBatch))));
         const int lmax = std::max(2 * kBatch * L0, 8);
         out.light_max[b] = lmax;
-        // light tasks: contiguous, at most task_nnz light nonzeros / kTaskSegs segments
+        // light tasks: contiguous, at most task_nnz light nonzeros / max_segs
+        // segments.  A light task does not start on a run of at least
+        // kSkipRun long segments (the list tasks own those): after the
+        // renumbering by length they are the instance's prefix, which the
+        // first task would otherwise walk one pointer round trip per pass of
+        // its lane groups (refinery LP with 168 periods: 1,344 long rows,
+        // 6.5 us per A x' phase on that warp).  A shorter run is walked in the
+        // task's first pass anyway and stays in it.
         int s = s0;
         while (s < s1) {
+            int run = 0;
+            while (s + run < s1 && ptr[s + run + 1] - ptr[s + run] > lmax) ++run;
+            if (run >= kSkipRun) {
+                s += run;
+                continue;
+            }
             int e = s;
             long long acc = 0;
-            while (e < s1 && e - s < kTaskSegs) {
+            while (e < s1 && e - s < max_segs) {
                 const int len = ptr[e + 1] - ptr[e];
                 const long long add = len > lmax ? 0 : len;
                 if (e > s && acc + add > task_nnz) break;
@@ -1379,6 +1404,9 @@ static int upload(DevMem& d, const void* h, size_t bytes, cudaStream_t s) {
     return SIH_PDHG_OK;
 }
 
+// One LP whose matrix (both sides, 16 bytes per nonzero) fits in half of L2.
+bool MixedSolver::latency_bound() const { return B_ == 1 && 16.0 * (double)nnz_ <= kSoloMaxBytes; }
+
 // Tasks, reduction groups, tickets, element chunks and active lists for SpMV
 // tasks of about `task_nnz` nonzeros (rebuilt by the autotuner).
 int MixedSolver::build_schedules(int task_nnz) {
@@ -1390,7 +1418,7 @@ int MixedSolver::build_schedules(int task_nnz) {
     SIHG_TRY(layout_.build(h_csr_ptr_, h_csc_ptr_, row_off_, col_off_,
                            SegMatrix{M_, csr_ptr_.as<int>(), csr_pairs_.as<int2>()},
                            SegMatrix{N_, csc_ptr_.as<int>(), csc_pairs_.as<int2>()}, task_nnz_, false, stream_,
-                           lanes_r_, lanes_c_));
+                           lanes_r_, lanes_c_, latency_bound() ? kSoloTaskSegs : kTaskSegs));
     rows_ = layout_.rows;
     cols_ = layout_.cols;
     chunks_all_ = layout_.chunks;
@@ -1684,7 +1712,7 @@ int MixedSolver::setup_persistent() {
     if (form < 0) {
         // automatic: the single-LP form for one LP whose matrix (both sides,
         // 16 bytes per nonzero) fits in half of L2: its steps are latency-bound
-        form = (B_ == 1 && 16.0 * (double)nnz_ <= kSoloMaxBytes) ? 2 : 0;
+        form = latency_bound() ? 2 : 0;
     }
     if (form == 2 && B_ != 1) form = 1;  // the single-LP form needs one LP
     return set_form(form);

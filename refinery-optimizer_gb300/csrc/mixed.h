@@ -103,7 +103,7 @@ struct SideSchedule {
 // light_lanes > 0 fixes the lanes per segment of the light tasks (a power of
 // two <= 32); 0 picks them from the task's mean segment length.
 void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out,
-                   int light_lanes = 0);
+                   int light_lanes = 0, int max_segs = kTaskSegs);
 
 // Device task layout of a block-diagonal (batched) matrix for the task engine
 // (warp.cuh): per side (rows = CSR for A x, columns = CSC for A^T y) the SpMV
@@ -117,7 +117,7 @@ class TaskLayout {
     // pass needed); otherwise the compaction kernels fill them.
     int build(const std::vector<int>& csr_ptr, const std::vector<int>& csc_ptr, const std::vector<int>& roff,
               const std::vector<int>& coff, const SegMatrix& rows_A, const SegMatrix& cols_A, int task_nnz,
-              bool all_active, cudaStream_t s, int row_lanes = 0, int col_lanes = 0);
+              bool all_active, cudaStream_t s, int row_lanes = 0, int col_lanes = 0, int max_segs = kTaskSegs);
 
     Side rows{}, cols{};
     Chunks chunks{};
@@ -178,6 +178,7 @@ class MixedSolver {
   private:
     int reset_state();
     int build_schedules(int task_nnz);
+    bool latency_bound() const;  // one LP small enough that its steps are latency-bound
     int autotune();
     int launch_compact(cudaStream_t s);
     int record_graph();
