@@ -101,7 +101,8 @@ struct SideSchedule {
 // Host: tasks of every instance of one side (light tasks of at most task_nnz
 // light nonzeros, then list tasks per length class) and their reduction groups.
 // light_lanes > 0 fixes the lanes per segment of the light tasks (a power of
-// two <= 32); 0 picks them from the task's mean segment length.
+// two <= 32); 0 picks them from the task's mean segment length.  max_segs caps
+// the segments of a light task (at most kTaskSegs).
 void make_schedule(const std::vector<int>& ptr, const std::vector<int>& inst_off, int task_nnz, SideSchedule& out,
                    int light_lanes = 0, int max_segs = kTaskSegs);
 
